@@ -1,0 +1,620 @@
+// extern "C" entry points of libfemflow_mpm.so (declared in include/femflow_mpm.h) and the host
+// code that sequences the kernels of a substep on the caller's stream.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <set>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+#include "mpm_kernels.cuh"
+
+namespace ffmpm {
+
+namespace {
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+int ilog2_ceil(int64_t v) {
+  int b = 0;
+  while ((int64_t(1) << b) < v) ++b;
+  return b;
+}
+
+int default_block_size(int dim, bool det) {
+  if (dim == 3) return det ? 4 : 8;
+  return det ? 8 : 16;
+}
+
+bool valid_params(const ffmpm_params* p) {
+  if (!p) return false;
+  if (p->dim != 2 && p->dim != 3) return false;
+  if (p->real_bytes != 4 && p->real_bytes != 8) return false;
+  if (p->res < 3 || p->res > 4096) return false;
+  if (p->model != FFMPM_MODEL_NEO_HOOKEAN && p->model != FFMPM_MODEL_SNOW) return false;
+  if (p->wall_mode != FFMPM_WALLS_REFERENCE && p->wall_mode != FFMPM_WALLS_STICKY3) return false;
+  if (p->block_size != 0 && (p->block_size < 2 || p->block_size > 16 || (p->block_size & (p->block_size - 1))))
+    return false;
+  return true;
+}
+
+}  // namespace
+
+bool make_layout(const ffmpm_params& p, int64_t n, Layout* L) {
+  if (!valid_params(&p) || n < 0 || n > int64_t(0x7FFFFFFF)) return false;
+  L->dim = p.dim;
+  L->real_bytes = p.real_bytes;
+  L->res = p.res;
+  L->R = p.res + 1;
+  L->bs = p.block_size ? p.block_size : default_block_size(p.dim, p.deterministic != 0);
+  L->nb = (L->R + L->bs - 1) / L->bs;
+  L->tile = L->bs + 2;
+  L->nblocks = p.dim == 3 ? int64_t(L->nb) * L->nb * L->nb : int64_t(L->nb) * L->nb;
+  L->nnodes = p.dim == 3 ? int64_t(L->R) * L->R * L->R : int64_t(L->R) * L->R;
+  L->cell_bits = p.deterministic ? p.dim * ilog2_ceil(L->bs) : 0;
+  L->key_bits = ilog2_ceil(L->nblocks) + L->cell_bits;
+  if (L->key_bits > 31) return false;
+  L->passes = std::max(1, (L->key_bits + 7) / 8);
+  L->n = n;
+  L->ntiles = std::max<int64_t>(1, (n + kRadixTile - 1) / kRadixTile);
+  L->max_chunks = (n + kChunk - 1) / kChunk + L->nblocks;
+  const size_t node_bytes = size_t(4) * p.real_bytes;
+  const int64_t tile_nodes = p.dim == 3 ? int64_t(L->tile) * L->tile * L->tile : int64_t(L->tile) * L->tile;
+  size_t off = sizeof(WsHeader);
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align_up(off + bytes, 256);
+    return o;
+  };
+  L->off_block_count = take(sizeof(uint32_t) * L->nblocks);
+  L->off_block_start = take(sizeof(uint32_t) * L->nblocks);
+  L->off_block_cnt = take(sizeof(uint32_t) * L->nblocks);
+  L->off_chunks = take(sizeof(int4) * L->max_chunks);
+  L->off_touched = take(sizeof(uint32_t) * L->nblocks);
+  L->off_occupied = take(sizeof(int4) * L->nblocks);
+  L->off_keys_next = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
+  L->off_keys0 = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
+  L->off_keys1 = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
+  L->off_vals0 = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
+  L->off_vals1 = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
+  L->off_hist = take(sizeof(uint32_t) * 256 * L->ntiles);
+  L->off_gridA = take(node_bytes * L->nnodes);
+  L->off_gridB = take(node_bytes * L->nnodes);
+  L->off_stage = take(p.deterministic ? node_bytes * tile_nodes * L->nblocks : 0);
+  L->total = off;
+  return true;
+}
+
+int sm_count() {
+  static int cached = 0;
+  if (!cached) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cached = v > 0 ? v : 148;
+  }
+  return cached;
+}
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+  });
+  return fn;
+}
+
+// Tensor map of a dense grid of Node4 records: dims (4 components, R, R[, R]) innermost first.
+bool encode_grid_map(CUtensorMap* map, void* base, const Layout& L) {
+  auto fn = encode_fn();
+  if (!fn) return false;
+  const CUtensorMapDataType dt = L.real_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  const cuuint64_t eb = L.real_bytes;
+  cuuint64_t dims[4] = {4, (cuuint64_t)L.R, (cuuint64_t)L.R, (cuuint64_t)L.R};
+  cuuint64_t strides[3] = {4 * eb, 4 * eb * L.R, 4 * eb * L.R * L.R};  // bytes, dims 1..rank-1
+  cuuint32_t box[4] = {4, (cuuint32_t)L.tile, (cuuint32_t)L.tile, (cuuint32_t)L.tile};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  const cuuint32_t rank = L.dim == 3 ? 4 : 3;
+  CUresult r = fn(map, dt, rank, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+template <typename T>
+KParams<T> kparams(const ffmpm_params& p) {
+  KParams<T> k;
+  k.dx = T(p.dx);
+  k.inv_dx = T(p.inv_dx);
+  k.dt = T(p.dt);
+  k.gravity = T(p.gravity);
+  k.volume = T(p.volume);
+  k.hardening = T(p.hardening);
+  k.mass = T(p.mass);
+  k.mu0 = T(p.mu_0);
+  k.lam0 = T(p.lambda_0);
+  k.v_allowed = T(p.dx * 0.9 / p.dt);  // three_d/grid_op.py:25, computed in double as the reference
+  k.res = p.res;
+  k.model = p.model;
+  k.wall_mode = p.wall_mode;
+  return k;
+}
+
+template <typename T>
+PView<T> pview(const ffmpm_particles& P) {
+  PView<T> v;
+  v.x = static_cast<T*>(P.x);
+  v.v = static_cast<T*>(P.v);
+  v.F = static_cast<T*>(P.F);
+  v.C = static_cast<T*>(P.C);
+  v.Jp = static_cast<T*>(P.Jp);
+  v.mass = static_cast<T*>(const_cast<void*>(P.mass));
+  v.mu0 = static_cast<T*>(const_cast<void*>(P.mu_0));
+  v.lam0 = static_cast<T*>(const_cast<void*>(P.lambda_0));
+  return v;
+}
+
+template <int DIM>
+Geom<DIM> geom(const Layout& L) {
+  Geom<DIM> g;
+  g.res = L.res;
+  g.R = L.R;
+  g.bs = L.bs;
+  g.nb = L.nb;
+  g.nblocks = (int)L.nblocks;
+  g.tile = L.tile;
+  return g;
+}
+
+struct Ws {
+  unsigned char* base;
+  WsHeader* hdr;
+  uint32_t *block_count, *block_start, *block_cnt, *touched, *keys_next, *keys0, *keys1, *vals0, *vals1, *hist;
+  int4 *chunks, *occupied;
+  void *gridA, *gridB, *stage;
+};
+
+Ws bind(void* ws, const Layout& L) {
+  Ws w;
+  w.base = static_cast<unsigned char*>(ws);
+  w.hdr = reinterpret_cast<WsHeader*>(w.base);
+  w.block_count = reinterpret_cast<uint32_t*>(w.base + L.off_block_count);
+  w.block_start = reinterpret_cast<uint32_t*>(w.base + L.off_block_start);
+  w.block_cnt = reinterpret_cast<uint32_t*>(w.base + L.off_block_cnt);
+  w.chunks = reinterpret_cast<int4*>(w.base + L.off_chunks);
+  w.touched = reinterpret_cast<uint32_t*>(w.base + L.off_touched);
+  w.occupied = reinterpret_cast<int4*>(w.base + L.off_occupied);
+  w.keys_next = reinterpret_cast<uint32_t*>(w.base + L.off_keys_next);
+  w.keys0 = reinterpret_cast<uint32_t*>(w.base + L.off_keys0);
+  w.keys1 = reinterpret_cast<uint32_t*>(w.base + L.off_keys1);
+  w.vals0 = reinterpret_cast<uint32_t*>(w.base + L.off_vals0);
+  w.vals1 = reinterpret_cast<uint32_t*>(w.base + L.off_vals1);
+  w.hist = reinterpret_cast<uint32_t*>(w.base + L.off_hist);
+  w.gridA = w.base + L.off_gridA;
+  w.gridB = w.base + L.off_gridB;
+  w.stage = w.base + L.off_stage;
+  return w;
+}
+
+int check_launch() {
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? FFMPM_OK : FFMPM_ERR_CUDA;
+}
+
+int work_grid(int64_t max_items, int per_sm) {
+  const int64_t cap = int64_t(sm_count()) * per_sm;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(max_items, cap));
+}
+
+// Optional per-phase CUDA-event timer of the profiling entry point.
+struct PhaseTimer {
+  std::vector<cudaEvent_t> ev;     // pairs (start, stop)
+  std::vector<int> phase;
+  std::vector<int> launches;
+  cudaStream_t s = nullptr;
+  void begin(int ph) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    ev.push_back(e0);
+    ev.push_back(e1);
+    phase.push_back(ph);
+  }
+  void end(int nlaunch) {
+    cudaEventRecord(ev.back(), s);
+    launches.push_back(nlaunch);
+  }
+  void collect(double* ms, int64_t* cnt) {
+    cudaStreamSynchronize(s);
+    for (size_t i = 0; i < phase.size(); ++i) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]);
+      ms[phase[i]] += t;
+      cnt[phase[i]] += launches[i];
+    }
+    for (auto e : ev) cudaEventDestroy(e);
+    ev.clear();
+  }
+};
+
+// keys -> sort -> plan.  Leaves the permutation pointer in *perm.
+template <int DIM, typename T>
+void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const T* x, bool keys_ready,
+                   const uint32_t** perm, cudaStream_t s, PhaseTimer* tm = nullptr) {
+  const KParams<T> kp = kparams<T>(p);
+  const Geom<DIM> g = geom<DIM>(L);
+  const uint32_t n = (uint32_t)L.n;
+  if (!keys_ready) {
+    if (tm) tm->begin(0);
+    k_keys<DIM, T><<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kp, g, x, n, L.cell_bits, w.keys_next,
+                                                                       w.block_count, &w.hdr->status);
+    if (tm) tm->end(1);
+  }
+  const uint32_t* ks = nullptr;
+  if (tm) tm->begin(1);
+  radix_sort(w.keys_next, n, L.passes, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, s, &ks, perm);
+  if (tm) tm->end(3 * L.passes);
+  if (tm) tm->begin(2);
+  k_plan<DIM><<<1, 1024, 0, s>>>(g, w.block_count, w.block_start, w.block_cnt, w.chunks, w.touched, w.occupied,
+                                 w.hdr);
+  if (tm) tm->end(1);
+}
+
+template <int DIM, typename T>
+size_t tile_smem(const Layout& L) {
+  const int64_t tn = DIM == 3 ? int64_t(L.tile) * L.tile * L.tile : int64_t(L.tile) * L.tile;
+  return size_t(tn) * 4 * sizeof(T);
+}
+
+// Raise a kernel's dynamic shared-memory limit once per kernel (a host-side attribute call,
+// kept out of CUDA-graph captures, which run after the first direct call).
+template <typename F>
+void set_smem(F* kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return;
+  static std::mutex mu;
+  static std::set<const void*> done;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.insert(reinterpret_cast<const void*>(kernel)).second)
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+template <int DIM, typename T, typename Sink>
+void launch_p2g(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<T>& P, const uint32_t* perm,
+                const Sink& sink, cudaStream_t s) {
+  const size_t smem = tile_smem<DIM, T>(L);
+  auto kern = k_p2g<DIM, T, Sink>;
+  set_smem(kern, smem);
+  kern<<<work_grid(L.max_chunks, 4), kThreads, smem, s>>>(kparams<T>(p), geom<DIM>(L), P, perm, w.chunks, w.hdr,
+                                                          sink, &w.hdr->status, &w.hdr->polar_fallbacks);
+}
+
+template <int DIM, typename T>
+void launch_grid_update(const ffmpm_params& p, const Layout& L, const Ws& w, cudaStream_t s) {
+  k_grid_update<DIM, T><<<work_grid(L.nblocks, 8), kThreads, 0, s>>>(
+      kparams<T>(p), geom<DIM>(L), w.touched, w.hdr, static_cast<Node4<T>*>(w.gridA), static_cast<Node4<T>*>(w.gridB));
+}
+
+template <int DIM, typename T, bool kTma, bool kSorted>
+int launch_g2p(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<T>& Pin, const PView<T>& Pout,
+               const uint32_t* perm, const T* user_gv, const G2PExtra& ex, cudaStream_t s) {
+  alignas(64) CUtensorMap map;
+  std::memset(&map, 0, sizeof(map));
+  if (kTma && !encode_grid_map(&map, w.gridB, L)) return FFMPM_ERR_CUDA;
+  const size_t smem = tile_smem<DIM, T>(L) + 128 + 16;  // + alignment pad + mbarrier
+  auto kern = k_g2p<DIM, T, kTma, kSorted>;
+  set_smem(kern, smem);
+  kern<<<work_grid(L.max_chunks, 4), kThreads, smem, s>>>(kparams<T>(p), geom<DIM>(L), Pin, Pout, perm, w.chunks,
+                                                          w.hdr, map, user_gv, ex, &w.hdr->status);
+  return FFMPM_OK;
+}
+
+// ------------------------------------------------------------------------------------ operations
+template <int DIM, typename T>
+int op_substep(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_particles* P, cudaStream_t s) {
+  const PView<T> pv = pview<T>(*P);
+  const uint32_t* perm = nullptr;
+  sort_and_plan<DIM, T>(p, L, w, pv.x, false, &perm, s);
+  launch_p2g<DIM, T>(p, L, w, pv, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s);
+  launch_grid_update<DIM, T>(p, L, w, s);
+  G2PExtra ex{};
+  int rc = launch_g2p<DIM, T, true, false>(p, L, w, pv, pv, perm, nullptr, ex, s);
+  return rc != FFMPM_OK ? rc : check_launch();
+}
+
+template <int DIM, typename T>
+int op_substeps_sorted(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_particles* a, ffmpm_particles* b,
+                       int32_t* ids_a, int32_t* ids_b, int nsteps, cudaStream_t s, PhaseTimer* tm = nullptr) {
+  PView<T> va = pview<T>(*a), vb = pview<T>(*b);
+  for (int k = 0; k < nsteps; ++k) {
+    const PView<T>& in = (k & 1) ? vb : va;
+    const PView<T>& out = (k & 1) ? va : vb;
+    const int32_t* ids_in = (k & 1) ? ids_b : ids_a;
+    int32_t* ids_out = (k & 1) ? ids_a : ids_b;
+    const uint32_t* perm = nullptr;
+    sort_and_plan<DIM, T>(p, L, w, in.x, k > 0, &perm, s, tm);
+    if (tm) tm->begin(3);
+    launch_p2g<DIM, T>(p, L, w, in, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s);
+    if (tm) tm->end(1);
+    if (tm) tm->begin(4);
+    launch_grid_update<DIM, T>(p, L, w, s);
+    if (tm) tm->end(1);
+    G2PExtra ex{ids_in, ids_out, w.keys_next, w.block_count, L.cell_bits};
+    if (tm) tm->begin(5);
+    int rc = launch_g2p<DIM, T, true, true>(p, L, w, in, out, perm, nullptr, ex, s);
+    if (tm) tm->end(1);
+    if (rc != FFMPM_OK) return rc;
+  }
+  // The last G2P counted the blocks of the final state for a substep that will not run here:
+  // clear the histogram so the workspace invariant (zero between calls) holds.
+  cudaMemsetAsync(w.block_count, 0, sizeof(uint32_t) * L.nblocks, s);
+  return check_launch();
+}
+
+template <int DIM, typename T>
+int op_p2g(const ffmpm_params& p, const Layout& L, const Ws& w, const ffmpm_particles* P, ffmpm_grid* grid,
+           cudaStream_t s) {
+  const PView<T> pv = pview<T>(*P);
+  const uint32_t* perm = nullptr;
+  sort_and_plan<DIM, T>(p, L, w, pv.x, false, &perm, s);
+  launch_p2g<DIM, T>(p, L, w, pv, perm, UserSink<T, DIM>{static_cast<T*>(grid->velocity), static_cast<T*>(grid->mass)},
+                     s);
+  return check_launch();
+}
+
+template <int DIM, typename T>
+int op_g2p(const ffmpm_params& p, const Layout& L, const Ws& w, const ffmpm_grid* grid, ffmpm_particles* P,
+           cudaStream_t s) {
+  const PView<T> pv = pview<T>(*P);
+  const uint32_t* perm = nullptr;
+  sort_and_plan<DIM, T>(p, L, w, pv.x, false, &perm, s);
+  G2PExtra ex{};
+  int rc = launch_g2p<DIM, T, false, false>(p, L, w, pv, pv, perm, static_cast<const T*>(grid->velocity), ex, s);
+  return rc != FFMPM_OK ? rc : check_launch();
+}
+
+template <int DIM, typename T>
+int op_grid_op(const ffmpm_params& p, ffmpm_grid* grid, cudaStream_t s) {
+  const int R = p.res + 1;
+  const int64_t nn = DIM == 3 ? int64_t(R) * R * R : int64_t(R) * R;
+  const int blocks = (int)std::min<int64_t>((nn + kThreads - 1) / kThreads, int64_t(sm_count()) * 16);
+  k_grid_op_dense<DIM, T><<<std::max(blocks, 1), kThreads, 0, s>>>(kparams<T>(p), R, static_cast<T*>(grid->velocity),
+                                                                   static_cast<const T*>(grid->mass));
+  return check_launch();
+}
+
+template <int DIM, typename T>
+int op_sort(const ffmpm_params& p, const Layout& L, const Ws& w, const void* x, uint32_t* keys_out,
+            uint32_t* perm_out, cudaStream_t s) {
+  const KParams<T> kp = kparams<T>(p);
+  const Geom<DIM> g = geom<DIM>(L);
+  const uint32_t n = (uint32_t)L.n;
+  k_keys<DIM, T><<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kp, g, static_cast<const T*>(x), n, L.cell_bits,
+                                                                     w.keys_next, nullptr, &w.hdr->status);
+  const uint32_t *ks = nullptr, *perm = nullptr;
+  radix_sort(w.keys_next, n, L.passes, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, s, &ks, &perm);
+  if (keys_out) cudaMemcpyAsync(keys_out, ks, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
+  if (perm_out) cudaMemcpyAsync(perm_out, perm, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
+  return check_launch();
+}
+
+template <int DIM, typename T>
+int op_diag(const ffmpm_params& p, const ffmpm_particles* P, double* out, cudaStream_t s) {
+  k_diag_init<<<1, 32, 0, s>>>(out);
+  const uint32_t n = (uint32_t)P->n;
+  const int blocks = std::max(1, (int)std::min<int64_t>((n + kThreads - 1) / kThreads, int64_t(sm_count()) * 8));
+  if (n > 0) k_diag<DIM, T><<<blocks, kThreads, 0, s>>>(kparams<T>(p), pview<T>(*P), n, out);
+  return check_launch();
+}
+
+// Dispatch on (dim, precision).
+template <template <int, typename> class Op, typename... Args>
+int dispatch(const ffmpm_params& p, Args&&... args) {
+  if (p.dim == 3) {
+    if (p.real_bytes == 4) return Op<3, float>::run(p, args...);
+    return Op<3, double>::run(p, args...);
+  }
+  if (p.real_bytes == 4) return Op<2, float>::run(p, args...);
+  return Op<2, double>::run(p, args...);
+}
+
+#define FFMPM_OP(NAME, FN)                                          \
+  template <int DIM, typename T>                                    \
+  struct NAME {                                                     \
+    template <typename... A>                                        \
+    static int run(const ffmpm_params& p, A&&... a) {               \
+      return FN<DIM, T>(p, a...);                                   \
+    }                                                               \
+  };
+FFMPM_OP(SubstepOp, op_substep)
+FFMPM_OP(SortedOp, op_substeps_sorted)
+FFMPM_OP(ProfileOp, op_substeps_sorted)
+FFMPM_OP(P2GOp, op_p2g)
+FFMPM_OP(G2POp, op_g2p)
+FFMPM_OP(GridOp, op_grid_op)
+FFMPM_OP(SortOp, op_sort)
+FFMPM_OP(DiagOp, op_diag)
+#undef FFMPM_OP
+
+bool particles_ok(const ffmpm_params& p, const ffmpm_particles* P, bool need_jp) {
+  if (!P || P->n < 0) return false;
+  if (P->n == 0) return true;
+  if (!P->x || !P->v || !P->F || !P->C) return false;
+  if (need_jp && !P->Jp) return false;
+  return true;
+}
+
+bool supported(const ffmpm_params& p) {
+  // 3D snow needs a device 3x3 SVD with clamping in G2P (three_d/g2p.py:48-58); not built.
+  return !(p.dim == 3 && p.model == FFMPM_MODEL_SNOW);
+}
+
+int prologue(const ffmpm_params* p, int64_t n, void* ws, size_t ws_bytes, Layout* L) {
+  if (!p || !make_layout(*p, n, L)) return FFMPM_ERR_BADARG;
+  if (!supported(*p)) return FFMPM_ERR_UNSUPPORTED;
+  if (p->deterministic) return FFMPM_ERR_UNSUPPORTED;
+  if (!ws || ws_bytes < L->total || (reinterpret_cast<uintptr_t>(ws) & 255)) return FFMPM_ERR_WORKSPACE;
+  return FFMPM_OK;
+}
+
+}  // namespace
+}  // namespace ffmpm
+
+using namespace ffmpm;
+
+extern "C" {
+
+const char* ffmpm_version(void) { return "femflow_gb300 mpm 0.1 (sm_103a)"; }
+
+int ffmpm_workspace_size(const ffmpm_params* p, int64_t n, size_t* bytes) {
+  Layout L;
+  if (!p || !bytes || !make_layout(*p, n, &L)) return FFMPM_ERR_BADARG;
+  *bytes = L.total;
+  return FFMPM_OK;
+}
+
+int ffmpm_workspace_init(const ffmpm_params* p, int64_t n, void* ws, size_t ws_bytes, void* stream) {
+  Layout L;
+  if (!p || !make_layout(*p, n, &L)) return FFMPM_ERR_BADARG;
+  if (!ws || ws_bytes < L.total) return FFMPM_ERR_WORKSPACE;
+  cudaMemsetAsync(ws, 0, L.total, static_cast<cudaStream_t>(stream));
+  return check_launch();
+}
+
+int ffmpm_status_read(void* ws, int32_t* status, uint32_t* polar_fallbacks, void* stream) {
+  if (!ws) return FFMPM_ERR_WORKSPACE;
+  WsHeader h;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (cudaMemcpyAsync(&h, ws, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess) return FFMPM_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return FFMPM_ERR_CUDA;
+  if (status) *status = h.status;
+  if (polar_fallbacks) *polar_fallbacks = h.polar_fallbacks;
+  return FFMPM_OK;
+}
+
+int ffmpm_status_clear(void* ws, void* stream) {
+  if (!ws) return FFMPM_ERR_WORKSPACE;
+  cudaMemsetAsync(ws, 0, 8, static_cast<cudaStream_t>(stream));  // status + polar_fallbacks
+  return check_launch();
+}
+
+int ffmpm_substep(const ffmpm_params* p, ffmpm_particles* P, void* ws, size_t ws_bytes, void* stream) {
+  Layout L;
+  if (!P) return FFMPM_ERR_BADARG;
+  int rc = prologue(p, P->n, ws, ws_bytes, &L);
+  if (rc != FFMPM_OK) return rc;
+  if (!particles_ok(*p, P, true)) return FFMPM_ERR_BADARG;
+  if (P->n == 0) return FFMPM_OK;
+  Ws w = bind(ws, L);
+  return dispatch<SubstepOp>(*p, L, w, P, static_cast<cudaStream_t>(stream));
+}
+
+int ffmpm_substeps_sorted(const ffmpm_params* p, ffmpm_particles* a, ffmpm_particles* b, int32_t* ids_a,
+                          int32_t* ids_b, int32_t nsteps, void* ws, size_t ws_bytes, void* stream) {
+  Layout L;
+  if (!a || !b || nsteps < 0 || a->n != b->n) return FFMPM_ERR_BADARG;
+  int rc = prologue(p, a->n, ws, ws_bytes, &L);
+  if (rc != FFMPM_OK) return rc;
+  if (!particles_ok(*p, a, true) || !particles_ok(*p, b, true)) return FFMPM_ERR_BADARG;
+  if ((a->mass != nullptr) != (b->mass != nullptr) || (a->mu_0 != nullptr) != (b->mu_0 != nullptr) ||
+      (a->lambda_0 != nullptr) != (b->lambda_0 != nullptr) || ((ids_a != nullptr) != (ids_b != nullptr)))
+    return FFMPM_ERR_BADARG;
+  if (a->n == 0 || nsteps == 0) return FFMPM_OK;
+  Ws w = bind(ws, L);
+  return dispatch<SortedOp>(*p, L, w, a, b, ids_a, ids_b, (int)nsteps, static_cast<cudaStream_t>(stream));
+}
+
+int ffmpm_profile_substeps(const ffmpm_params* p, ffmpm_particles* a, ffmpm_particles* b, int32_t* ids_a,
+                           int32_t* ids_b, int32_t nsteps, void* ws, size_t ws_bytes, void* stream, double* phase_ms,
+                           int64_t* phase_launches) {
+  Layout L;
+  if (!a || !b || nsteps < 0 || a->n != b->n || !phase_ms || !phase_launches) return FFMPM_ERR_BADARG;
+  int rc = prologue(p, a->n, ws, ws_bytes, &L);
+  if (rc != FFMPM_OK) return rc;
+  if (!particles_ok(*p, a, true) || !particles_ok(*p, b, true)) return FFMPM_ERR_BADARG;
+  if (a->n == 0 || nsteps == 0) return FFMPM_OK;
+  Ws w = bind(ws, L);
+  PhaseTimer tm;
+  tm.s = static_cast<cudaStream_t>(stream);
+  rc = dispatch<ProfileOp>(*p, L, w, a, b, ids_a, ids_b, (int)nsteps, tm.s, &tm);
+  tm.collect(phase_ms, phase_launches);
+  return rc;
+}
+
+int ffmpm_plan_info(const ffmpm_params* p, int64_t n, int64_t* info) {
+  Layout L;
+  if (!p || !info || !make_layout(*p, n, &L)) return FFMPM_ERR_BADARG;
+  info[0] = L.bs;
+  info[1] = L.nb;
+  info[2] = L.nblocks;
+  info[3] = L.key_bits;
+  info[4] = L.passes;
+  info[5] = 3 * L.passes + 4;  // radix passes x (hist, scan, scatter) + plan + P2G + grid + G2P
+  info[6] = L.tile;
+  info[7] = L.max_chunks;
+  return FFMPM_OK;
+}
+
+int ffmpm_p2g(const ffmpm_params* p, const ffmpm_particles* P, ffmpm_grid* grid, void* ws, size_t ws_bytes,
+              void* stream) {
+  Layout L;
+  if (!P || !grid || !grid->velocity || !grid->mass) return FFMPM_ERR_BADARG;
+  int rc = prologue(p, P->n, ws, ws_bytes, &L);
+  if (rc != FFMPM_OK) return rc;
+  if (!particles_ok(*p, P, p->model == FFMPM_MODEL_SNOW)) return FFMPM_ERR_BADARG;
+  if (P->n == 0) return FFMPM_OK;
+  Ws w = bind(ws, L);
+  return dispatch<P2GOp>(*p, L, w, P, grid, static_cast<cudaStream_t>(stream));
+}
+
+int ffmpm_grid_op(const ffmpm_params* p, ffmpm_grid* grid, void* stream) {
+  Layout L;
+  if (!p || !make_layout(*p, 0, &L)) return FFMPM_ERR_BADARG;
+  if (!grid || !grid->velocity || !grid->mass) return FFMPM_ERR_BADARG;
+  return dispatch<GridOp>(*p, grid, static_cast<cudaStream_t>(stream));
+}
+
+int ffmpm_g2p(const ffmpm_params* p, const ffmpm_grid* grid, ffmpm_particles* P, void* ws, size_t ws_bytes,
+              void* stream) {
+  Layout L;
+  if (!P || !grid || !grid->velocity) return FFMPM_ERR_BADARG;
+  int rc = prologue(p, P->n, ws, ws_bytes, &L);
+  if (rc != FFMPM_OK) return rc;
+  if (!particles_ok(*p, P, p->dim == 2 || p->model == FFMPM_MODEL_SNOW)) return FFMPM_ERR_BADARG;
+  if (P->n == 0) return FFMPM_OK;
+  Ws w = bind(ws, L);
+  return dispatch<G2POp>(*p, L, w, grid, P, static_cast<cudaStream_t>(stream));
+}
+
+int ffmpm_sort_by_block(const ffmpm_params* p, const void* x, int64_t n, uint32_t* keys_out, uint32_t* perm_out,
+                        void* ws, size_t ws_bytes, void* stream) {
+  Layout L;
+  if (!p || !make_layout(*p, n, &L)) return FFMPM_ERR_BADARG;
+  if (!ws || ws_bytes < L.total || (reinterpret_cast<uintptr_t>(ws) & 255)) return FFMPM_ERR_WORKSPACE;
+  if (n == 0) return FFMPM_OK;
+  if (!x) return FFMPM_ERR_BADARG;
+  Ws w = bind(ws, L);
+  return dispatch<SortOp>(*p, L, w, x, keys_out, perm_out, static_cast<cudaStream_t>(stream));
+}
+
+int ffmpm_diagnostics_fp64(const ffmpm_params* p, const ffmpm_particles* P, double* out, void* stream) {
+  Layout L;
+  if (!p || !make_layout(*p, 0, &L) || !P || !out) return FFMPM_ERR_BADARG;
+  if (P->n > 0 && (!P->x || !P->v || !P->F)) return FFMPM_ERR_BADARG;
+  return dispatch<DiagOp>(*p, P, out, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,319 @@
+// Shared device code for the MLS-MPM substep kernels (sm_103a).
+//
+// Reference semantics (FEMFlow, femflow/solvers/mpm/...):
+//   quadratic B-spline weights          three_d/p2g.py:55
+//   base = int64(x*inv_dx - 0.5)        three_d/p2g.py:50 (truncation toward zero)
+//   fixed-corotated stress + APIC       utils.py:95-135 (3D), utils.py:52-92 (2D)
+//   polar decomposition                 numerics/linear_algebra.py:96-135
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/femflow_mpm.h"
+
+namespace ffmpm {
+
+constexpr int kThreads = 256;
+
+// ----------------------------------------------------------------------------------------------
+// Precision traits
+template <typename T>
+struct alignas(4 * sizeof(T)) Node4 {
+  T x, y, z, w;
+};
+
+template <typename T>
+__device__ __forceinline__ T ffabs(T a) { return a < T(0) ? -a : a; }
+__device__ __forceinline__ float ffsqrt(float a) { return sqrtf(a); }
+__device__ __forceinline__ double ffsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ float ffexp(float a) { return expf(a); }
+__device__ __forceinline__ double ffexp(double a) { return exp(a); }
+template <typename T>
+__device__ __forceinline__ T ffclamp(T v, T lo, T hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+template <typename T>
+struct Eps;
+template <>
+struct Eps<float> {
+  static constexpr float value = 1.1920929e-07f;
+};
+template <>
+struct Eps<double> {
+  static constexpr double value = 2.220446049250313e-16;
+};
+
+// ----------------------------------------------------------------------------------------------
+// Status word (device side).  Bits of FFMPM_STATUS_* are OR-ed in; the host reads it after sync.
+__device__ __forceinline__ void raise_status(int32_t* status, int32_t bit) {
+  if (status) atomicOr(status, bit);
+}
+
+// ----------------------------------------------------------------------------------------------
+// Grid geometry shared by all kernels.  Nodes per axis R = res + 1.  The grid is split into
+// cubic (square in 2D) blocks of BS nodes per axis for work assignment: a particle belongs to the
+// block that holds its base node, and its 3-node stencil then stays inside the block's tile of
+// BS+2 nodes per axis.
+template <int DIM>
+struct Geom {
+  int res;     // grid resolution
+  int R;       // nodes per axis
+  int bs;      // block side (nodes)
+  int nb;      // blocks per axis = ceil(R / bs)
+  int nblocks; // nb^DIM
+  int tile;    // bs + 2
+};
+
+// ----------------------------------------------------------------------------------------------
+// Base node and fractional offset, following the reference's truncation (astype(int64)).
+// Returns false for out-of-range or non-finite coordinates (the reference raises RuntimeError).
+// Products and differences here are rounded separately (no FMA contraction), as numpy computes
+// `pos * inv_dx - 0.5`, so the base node is reproducible bit for bit on the host.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+template <typename T>
+__device__ __forceinline__ bool base_of(T x, T inv_dx, int res, int& b, T& fx) {
+  const T xs = mul_rn(x, inv_dx);
+  const T t = sub_rn(xs, T(0.5));
+  if (!(t > T(-1) && t < T(res))) return false;
+  b = static_cast<int>(t);  // truncation toward zero, as numpy astype(int64)
+  if (b < 0 || b + 2 > res) return false;
+  fx = sub_rn(xs, T(b));
+  return true;
+}
+
+template <typename T>
+__device__ __forceinline__ void bspline(T fx, T w[3]) {
+  const T a = T(1.5) - fx, b = fx - T(1), c = fx - T(0.5);
+  w[0] = T(0.5) * a * a;
+  w[1] = T(0.75) - b * b;
+  w[2] = T(0.5) * c * c;
+}
+
+// ----------------------------------------------------------------------------------------------
+// Small dense matrix helpers (row-major).
+template <typename T>
+__device__ __forceinline__ T det3(const T m[9]) {
+  return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+         m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+template <typename T>
+__device__ __forceinline__ void cofactor3(const T m[9], T c[9]) {
+  c[0] = m[4] * m[8] - m[5] * m[7];
+  c[1] = m[5] * m[6] - m[3] * m[8];
+  c[2] = m[3] * m[7] - m[4] * m[6];
+  c[3] = m[2] * m[7] - m[1] * m[8];
+  c[4] = m[0] * m[8] - m[2] * m[6];
+  c[5] = m[1] * m[6] - m[0] * m[7];
+  c[6] = m[1] * m[5] - m[2] * m[4];
+  c[7] = m[2] * m[3] - m[0] * m[5];
+  c[8] = m[0] * m[4] - m[1] * m[3];
+}
+
+// Orthogonal polar factor R of F (F = R S, S symmetric positive definite) by Newton's iteration
+// X <- (g X + X^{-T}/g)/2 with Frobenius-norm scaling g (Higham 1986, "Computing the polar
+// decomposition - with applications").  The iteration converges to the unique orthogonal polar
+// factor of any nonsingular F, including det F < 0, where R is a reflection exactly as
+// U @ Vh from an SVD (linear_algebra.py:131-132).  Returns the number of iterations, or -1 when F
+// is (numerically) singular or the iteration did not settle.
+template <typename T>
+__device__ __forceinline__ int polar3_newton(const T F[9], T R[9], int max_iter) {
+  T X[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) X[i] = F[i];
+  const T tol = T(8) * Eps<T>::value;
+  for (int it = 0; it < max_iter; ++it) {
+    T cof[9];
+    cofactor3(X, cof);
+    const T det = X[0] * cof[0] + X[1] * cof[1] + X[2] * cof[2];
+    T nx = 0, nc = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      nx += X[i] * X[i];
+      nc += cof[i] * cof[i];
+    }
+    if (!(ffabs(det) > T(0)) || !(nx > T(0))) return -1;
+    const T inv_det = T(1) / det;
+    // ||X^{-T}||_F = ||cof||_F / |det|;  g = sqrt(||X^{-1}|| / ||X||)
+    T g = ffsqrt(ffsqrt(nc * inv_det * inv_det / nx));
+    const T ha = T(0.5) * g, hb = T(0.5) * inv_det / g;
+    T diff = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const T xn = ha * X[i] + hb * cof[i];
+      const T d = xn - X[i];
+      diff += d * d;
+      X[i] = xn;
+    }
+    if (diff <= tol * tol * T(3)) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) R[i] = X[i];
+      return it + 1;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R[i] = X[i];
+  return -1;
+}
+
+// Polar factor used by the stress.  In float, F whose smallest singular value is small relative
+// to its largest (|det F| / (|F|_F/sqrt 3)^3 below 1e-3) or where the float iteration fails is
+// redone in double; `fallbacks` counts those particles.
+template <typename T>
+__device__ __forceinline__ void polar3(const T F[9], T R[9], uint32_t* fallbacks) {
+  if constexpr (sizeof(T) == 4) {
+    T n2 = 0;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) n2 += F[i] * F[i];
+    const T d = det3(F);
+    const T s3 = n2 * ffsqrt(n2) * T(0.19245009);  // (|F|_F / sqrt 3)^3 = |F|_F^3 / 5.196
+    bool need64 = !(ffabs(d) > T(1e-3) * s3);
+    if (!need64) need64 = polar3_newton(F, R, 12) < 0;
+    if (need64) {
+      double Fd[9], Rd[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) Fd[i] = double(F[i]);
+      polar3_newton(Fd, Rd, 60);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) R[i] = T(Rd[i]);
+      if (fallbacks) atomicAdd(fallbacks, 1u);
+    }
+  } else {
+    // double: a failure means F is singular to working precision; the last iterate is kept (the
+    // reference's LAPACK answer is arbitrary in the null space there) and counted.
+    if (polar3_newton(F, R, 60) < 0 && fallbacks) atomicAdd(fallbacks, 1u);
+  }
+}
+
+// linear_algebra.py:96-116 (2D closed form with +1e-10 in the denominator).
+template <typename T>
+__device__ __forceinline__ void polar2(const T m[4], T r[4]) {
+  const T x = m[0] + m[3];
+  const T y = m[2] - m[1];
+  const T denom = ffsqrt(x * x + y * y) + T(1e-10);
+  const T scale = T(1) / denom;
+  const T c = x * scale, s = y * scale;
+  r[0] = c;
+  r[1] = -s;
+  r[2] = s;
+  r[3] = c;
+}
+
+// 2x2 SVD F = U diag(s) V^T, s >= 0 descending, by the two-angle closed form.
+template <typename T>
+__device__ __forceinline__ void svd2(const T F[4], T U[4], T s[2], T V[4]) {
+  const T a = F[0], b = F[1], c = F[2], d = F[3];
+  const T E = T(0.5) * (a + d), Fh = T(0.5) * (a - d), G = T(0.5) * (c + b), H = T(0.5) * (c - b);
+  const T Q = ffsqrt(E * E + H * H), Rr = ffsqrt(Fh * Fh + G * G);
+  T s1 = Q + Rr, s2 = Q - Rr;
+  const T a1 = atan2(G, Fh), a2 = atan2(H, E);
+  const T th = T(0.5) * (a2 - a1), ph = T(0.5) * (a2 + a1);
+  T su, cu, sv, cv;
+  if constexpr (sizeof(T) == 4) {
+    sincosf(ph, &su, &cu);
+    sincosf(th, &sv, &cv);
+  } else {
+    sincos(ph, &su, &cu);
+    sincos(th, &sv, &cv);
+  }
+  U[0] = cu; U[1] = -su; U[2] = su; U[3] = cu;
+  V[0] = cv; V[1] = sv; V[2] = -sv; V[3] = cv;
+  if (s2 < T(0)) {
+    s2 = -s2;
+    U[1] = -U[1];
+    U[3] = -U[3];
+  }
+  s[0] = s1;
+  s[1] = s2;
+}
+
+// ----------------------------------------------------------------------------------------------
+// Warp helpers
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Add 1 to counts[key] for every lane with valid=true, one atomic per distinct key in the warp.
+__device__ __forceinline__ void warp_count(unsigned* counts, unsigned key, bool valid) {
+  const unsigned active = __activemask();
+  const unsigned vmask = __ballot_sync(active, valid);
+  if (!valid) return;
+  const unsigned peers = __match_any_sync(vmask, key);
+  const int leader = __ffs(peers) - 1;
+  if ((threadIdx.x & 31) == leader) atomicAdd(&counts[key], (unsigned)__popc(peers));
+}
+
+// ----------------------------------------------------------------------------------------------
+// Vector atomics into global memory.
+__device__ __forceinline__ void atomic_add4(Node4<float>* p, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
+               : "memory");
+}
+__device__ __forceinline__ void atomic_add4(Node4<double>* p, double a, double b, double c, double d) {
+  atomicAdd(&p->x, a);
+  atomicAdd(&p->y, b);
+  atomicAdd(&p->z, c);
+  atomicAdd(&p->w, d);
+}
+
+// ----------------------------------------------------------------------------------------------
+// mbarrier + TMA (cp.async.bulk.tensor) wrappers.  Every wait is bounded: after kSpinLimit polls
+// the caller records FFMPM_STATUS_TIMEOUT and gives up instead of hanging the GPU.
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_shared() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// Returns true once the phase with the given parity has completed; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t addr = smem_u32(bar);
+  for (uint32_t i = 0; i < kSpinLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_4d(void* smem_dst, const void* tmap, uint64_t* bar, int c0, int c1,
+                                            int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5, %6}], [%2];" ::"r"(smem_u32(smem_dst)),
+      "l"(tmap), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void* smem_dst, const void* tmap, uint64_t* bar, int c0, int c1,
+                                            int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(smem_dst)),
+      "l"(tmap), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+}  // namespace ffmpm

@@ -1,0 +1,839 @@
+// MLS-MPM substep kernels, templated on dimension (2, 3) and precision (float, double).
+//
+// Pipeline of one substep (all on one stream):
+//   k_keys         block key of every particle (three_d/p2g.py:50 base rule) + block histogram
+//   radix sort     stable, bit-exact permutation by key (sort.cu)
+//   k_plan         block offsets, work chunks, touched-block list (one CTA)
+//   k_p2g          stress + 3^d-node scatter into a shared-memory tile per block, one vector
+//                  atomic per touched node on flush          (three_d/p2g.py:14-80)
+//   k_grid_update  momentum -> velocity, gravity, clamp, walls over touched blocks only
+//                                                            (three_d/grid_op.py:5-47)
+//   k_g2p          TMA-staged tile of grid velocities, gather v and APIC C, advect, update F
+//                                                            (three_d/g2p.py:9-59)
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace ffmpm {
+
+template <typename T>
+struct KParams {
+  T dx, inv_dx, dt, gravity, volume, hardening, mass, mu0, lam0, v_allowed;
+  int res, model, wall_mode;
+};
+
+template <typename T>
+struct PView {
+  T *x, *v, *F, *C, *Jp;
+  T *mass, *mu0, *lam0;  // nullable: scalar material from KParams
+};
+
+template <int DIM>
+__device__ __forceinline__ void block_coords(const Geom<DIM>& g, int blk, int c[DIM]) {
+  if constexpr (DIM == 3) {
+    c[2] = blk % g.nb;
+    c[1] = (blk / g.nb) % g.nb;
+    c[0] = blk / (g.nb * g.nb);
+  } else {
+    c[1] = blk % g.nb;
+    c[0] = blk / g.nb;
+  }
+}
+
+template <int DIM>
+__device__ __forceinline__ int64_t node_index(int R, const int I[DIM]) {
+  if constexpr (DIM == 3)
+    return ((int64_t)I[0] * R + I[1]) * (int64_t)R + I[2];
+  else
+    return (int64_t)I[0] * R + I[1];
+}
+
+// Key of a particle: block id (and, with cell_bits > 0, the cell inside the block in the low bits).
+template <int DIM, typename T>
+__device__ __forceinline__ bool particle_key(const T* xp, const KParams<T>& kp, const Geom<DIM>& g, int cell_bits,
+                                             uint32_t& key, uint32_t& blk) {
+  int b[DIM];
+  bool ok = true;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    T fx;
+    ok = ok && base_of(xp[d], kp.inv_dx, kp.res, b[d], fx);
+  }
+  if (!ok) {
+    key = kInvalidKey;
+    blk = 0;
+    return false;
+  }
+  uint32_t bid = 0, cell = 0;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    bid = bid * g.nb + (uint32_t)(b[d] / g.bs);
+    cell = cell * g.bs + (uint32_t)(b[d] % g.bs);
+  }
+  blk = bid;
+  key = cell_bits ? ((bid << cell_bits) | cell) : bid;
+  return true;
+}
+
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kThreads) k_keys(KParams<T> kp, Geom<DIM> g, const T* __restrict__ x, uint32_t n,
+                                                   int cell_bits, uint32_t* __restrict__ keys,
+                                                   uint32_t* __restrict__ block_count, int32_t* status) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool valid = false;
+  uint32_t key = kInvalidKey, blk = 0;
+  if (i < n) {
+    T xp[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) xp[d] = x[(size_t)i * DIM + d];
+    valid = particle_key<DIM, T>(xp, kp, g, cell_bits, key, blk);
+    if (!valid) raise_status(status, FFMPM_STATUS_OOB);
+    keys[i] = key;
+  }
+  if (block_count) warp_count(block_count, blk, valid);
+}
+
+// ----------------------------------------------------------------------------------------------
+// k_plan: one CTA of 1024 threads over all blocks.  Produces block starts (exclusive scan of the
+// histogram), chunks of at most kChunk particles, the list of occupied blocks, and the touched
+// blocks (occupied blocks dilated by +1 along every axis, because a stencil based in block b
+// reaches 2 nodes into block b+1).  Re-zeroes the histogram for the next substep.
+struct Scan4 {
+  uint32_t a, b, c, d;
+};
+
+__device__ __forceinline__ Scan4 block_exclusive_scan4(Scan4 v, Scan4* total, Scan4* warp_buf) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  Scan4 inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t ta = __shfl_up_sync(0xffffffffu, inc.a, o), tb = __shfl_up_sync(0xffffffffu, inc.b, o);
+    const uint32_t tc = __shfl_up_sync(0xffffffffu, inc.c, o), td = __shfl_up_sync(0xffffffffu, inc.d, o);
+    if (lane >= o) {
+      inc.a += ta; inc.b += tb; inc.c += tc; inc.d += td;
+    }
+  }
+  if (lane == 31) warp_buf[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    Scan4 w = lane < nwarps ? warp_buf[lane] : Scan4{0, 0, 0, 0};
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t ta = __shfl_up_sync(0xffffffffu, w.a, o), tb = __shfl_up_sync(0xffffffffu, w.b, o);
+      const uint32_t tc = __shfl_up_sync(0xffffffffu, w.c, o), td = __shfl_up_sync(0xffffffffu, w.d, o);
+      if (lane >= o) {
+        w.a += ta; w.b += tb; w.c += tc; w.d += td;
+      }
+    }
+    if (lane < nwarps) warp_buf[lane] = w;
+  }
+  __syncthreads();
+  Scan4 prev = warp > 0 ? warp_buf[warp - 1] : Scan4{0, 0, 0, 0};
+  Scan4 ex{prev.a + inc.a - v.a, prev.b + inc.b - v.b, prev.c + inc.c - v.c, prev.d + inc.d - v.d};
+  *total = warp_buf[nwarps - 1];
+  __syncthreads();
+  return ex;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(1024) k_plan(Geom<DIM> g, uint32_t* __restrict__ block_count,
+                                               uint32_t* __restrict__ block_start, uint32_t* __restrict__ block_cnt,
+                                               int4* __restrict__ chunks, uint32_t* __restrict__ touched,
+                                               int4* __restrict__ occupied, WsHeader* hdr) {
+  __shared__ Scan4 warp_buf[32];
+  Scan4 carry{0, 0, 0, 0};  // (particles, chunks, touched, occupied)
+  for (int seg = 0; seg < g.nblocks; seg += blockDim.x) {
+    const int b = seg + threadIdx.x;
+    uint32_t c = 0, tch = 0;
+    if (b < g.nblocks) {
+      c = block_count[b];
+      int bc[DIM];
+      block_coords<DIM>(g, b, bc);
+      // touched if any block b - o, o in {0,1}^DIM, holds particles
+#pragma unroll
+      for (int o = 0; o < (1 << DIM); ++o) {
+        int nb_id = 0;
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const int cc = bc[d] - ((o >> (DIM - 1 - d)) & 1);
+          ok = ok && cc >= 0;
+          nb_id = nb_id * g.nb + cc;
+        }
+        if (ok && block_count[nb_id] > 0) tch = 1;
+      }
+    }
+    const uint32_t nch = (c + kChunk - 1) / kChunk;
+    Scan4 v{c, nch, tch, c > 0 ? 1u : 0u}, tot;
+    Scan4 ex = block_exclusive_scan4(v, &tot, warp_buf);
+    if (b < g.nblocks) {
+      const uint32_t start = carry.a + ex.a;
+      block_start[b] = start;
+      block_cnt[b] = c;
+      for (uint32_t q = 0; q < nch; ++q) {
+        const uint32_t s = start + q * kChunk;
+        chunks[carry.b + ex.b + q] = make_int4(b, (int)s, (int)min((uint32_t)kChunk, c - q * kChunk), 0);
+      }
+      if (tch) touched[carry.c + ex.c] = (uint32_t)b;
+      if (c > 0) occupied[carry.d + ex.d] = make_int4(b, (int)start, (int)c, 0);
+    }
+    carry.a += tot.a; carry.b += tot.b; carry.c += tot.c; carry.d += tot.d;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    hdr->n_valid = carry.a;
+    hdr->n_chunks = carry.b;
+    hdr->n_touched = carry.c;
+    hdr->n_occupied = carry.d;
+  }
+  for (int b = threadIdx.x; b < g.nblocks; b += blockDim.x) block_count[b] = 0;
+}
+
+// ----------------------------------------------------------------------------------------------
+// Grid-side scatter targets of P2G.
+template <typename T>
+struct InternalSink {  // workspace grid of Node4 {momentum xyz, mass}
+  Node4<T>* A;
+  __device__ __forceinline__ void add(int64_t node, T a, T b, T c, T m) const {
+    if constexpr (sizeof(T) == 4) {
+      atomicAdd(reinterpret_cast<float4*>(A + node), make_float4(a, b, c, m));
+    } else {
+      atomic_add4(A + node, a, b, c, m);
+    }
+  }
+};
+
+template <typename T, int DIM>
+struct UserSink {  // caller's grid_velocity [nodes][DIM] and grid_mass [nodes]
+  T* gv;
+  T* gm;
+  __device__ __forceinline__ void add(int64_t node, T a, T b, T c, T m) const {
+    atomicAdd(&gv[node * DIM + 0], a);
+    atomicAdd(&gv[node * DIM + 1], b);
+    if constexpr (DIM == 3) atomicAdd(&gv[node * DIM + 2], c);
+    atomicAdd(&gm[node], m);
+  }
+};
+
+template <int DIM>
+__device__ __forceinline__ int tile_nodes(const Geom<DIM>& g) {
+  return DIM == 3 ? g.tile * g.tile * g.tile : g.tile * g.tile;
+}
+
+// Stress + APIC affine matrix of one particle (utils.py:95-135 / 52-92):
+//   A = -(dt*vol) * (4*inv_dx^2 * PF) + m*C,  PF = 2mu(F-R)F^T + lam(J-1)J  (scalar on all entries)
+template <int DIM, typename T>
+__device__ __forceinline__ void affine_of(const KParams<T>& kp, const T* F, const T* C, T m, T mu, T lam, T* A,
+                                          uint32_t* fallbacks) {
+  const T Dinv = T(4) * kp.inv_dx * kp.inv_dx;
+  const T s = -(kp.dt * kp.volume);
+  if constexpr (DIM == 3) {
+    T R[9];
+    polar3<T>(F, R, fallbacks);
+    const T J = det3(F);
+    const T sc = lam * (J - T(1)) * J;
+    T FmR[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) FmR[i] = T(2) * mu * (F[i] - R[i]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const T pf = FmR[i * 3 + 0] * F[j * 3 + 0] + FmR[i * 3 + 1] * F[j * 3 + 1] + FmR[i * 3 + 2] * F[j * 3 + 2] + sc;
+        A[i * 3 + j] = s * (Dinv * pf) + m * C[i * 3 + j];
+      }
+  } else {
+    T R[4];
+    polar2<T>(F, R);
+    const T J = F[0] * F[3] - F[1] * F[2];
+    const T sc = lam * (J - T(1)) * J;
+    T FmR[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) FmR[i] = T(2) * mu * (F[i] - R[i]);
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const T pf = FmR[i * 2 + 0] * F[j * 2 + 0] + FmR[i * 2 + 1] * F[j * 2 + 1] + sc;
+        A[i * 2 + j] = s * (Dinv * pf) + m * C[i * 2 + j];
+      }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void lame_of(const KParams<T>& kp, const PView<T>& P, uint32_t p, T& m, T& mu, T& lam) {
+  m = P.mass ? P.mass[p] : kp.mass;
+  const T mu0 = P.mu0 ? P.mu0[p] : kp.mu0;
+  const T lam0 = P.lam0 ? P.lam0[p] : kp.lam0;
+  const T e = (kp.model == FFMPM_MODEL_SNOW) ? ffexp(kp.hardening * (T(1) - P.Jp[p])) : kp.hardening;
+  mu = mu0 * e;
+  lam = lam0 * e;
+}
+
+// Scatter one particle into the shared tile (SoA: 4 arrays of TN values).
+template <int DIM, typename T>
+__device__ __forceinline__ void p2g_particle(const KParams<T>& kp, const Geom<DIM>& g, const PView<T>& P, uint32_t p,
+                                             const int org[DIM], T* tile, int TN, int32_t* status,
+                                             uint32_t* fallbacks) {
+  constexpr int DD = DIM * DIM;
+  T fx[DIM], w[3][DIM];
+  int lb[DIM];
+  bool ok = true;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    int b;
+    ok = ok && base_of(P.x[(size_t)p * DIM + d], kp.inv_dx, kp.res, b, fx[d]);
+    lb[d] = b - org[d];
+    ok = ok && lb[d] >= 0 && lb[d] + 2 < g.tile;
+    T ww[3];
+    bspline(fx[d], ww);
+    w[0][d] = ww[0];
+    w[1][d] = ww[1];
+    w[2][d] = ww[2];
+  }
+  if (!ok) {
+    raise_status(status, FFMPM_STATUS_OOB);
+    return;
+  }
+  T m, mu, lam;
+  lame_of(kp, P, p, m, mu, lam);
+  T F[DD], C[DD], A[DD], v[DIM];
+#pragma unroll
+  for (int i = 0; i < DD; ++i) {
+    F[i] = P.F[(size_t)p * DD + i];
+    C[i] = P.C[(size_t)p * DD + i];
+  }
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) v[d] = P.v[(size_t)p * DIM + d];
+  affine_of<DIM, T>(kp, F, C, m, mu, lam, A, fallbacks);
+  const T dx = kp.dx;
+  T mv[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) mv[d] = v[d] * m;
+  if constexpr (DIM == 3) {
+    const int T1 = g.tile;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const T d0 = (T(i) - fx[0]) * dx;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const T d1 = (T(j) - fx[1]) * dx;
+        const T wij = w[i][0] * w[j][1];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const T d2 = (T(k) - fx[2]) * dx;
+          const T weight = wij * w[k][2];
+          const int idx = ((lb[0] + i) * T1 + (lb[1] + j)) * T1 + (lb[2] + k);
+          atomicAdd(&tile[idx], weight * (mv[0] + (A[0] * d0 + A[1] * d1 + A[2] * d2)));
+          atomicAdd(&tile[TN + idx], weight * (mv[1] + (A[3] * d0 + A[4] * d1 + A[5] * d2)));
+          atomicAdd(&tile[2 * TN + idx], weight * (mv[2] + (A[6] * d0 + A[7] * d1 + A[8] * d2)));
+          atomicAdd(&tile[3 * TN + idx], weight * m);
+        }
+      }
+    }
+  } else {
+    const int T1 = g.tile;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const T d0 = (T(i) - fx[0]) * dx;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const T d1 = (T(j) - fx[1]) * dx;
+        const T weight = w[i][0] * w[j][1];
+        const int idx = (lb[0] + i) * T1 + (lb[1] + j);
+        atomicAdd(&tile[idx], weight * (mv[0] + (A[0] * d0 + A[1] * d1)));
+        atomicAdd(&tile[TN + idx], weight * (mv[1] + (A[2] * d0 + A[3] * d1)));
+        atomicAdd(&tile[3 * TN + idx], weight * m);
+      }
+    }
+  }
+}
+
+template <int DIM, typename T, typename Sink>
+__device__ __forceinline__ void p2g_flush(const T* tile, int TN, const Geom<DIM>& g, const int org[DIM],
+                                          const Sink& sink) {
+  const int T1 = g.tile;
+  for (int t = threadIdx.x; t < TN; t += blockDim.x) {
+    const T a = tile[t], b = tile[TN + t], c = tile[2 * TN + t], m = tile[3 * TN + t];
+    if (a == T(0) && b == T(0) && c == T(0) && m == T(0)) continue;
+    int I[DIM];
+    if constexpr (DIM == 3) {
+      I[0] = org[0] + t / (T1 * T1);
+      I[1] = org[1] + (t / T1) % T1;
+      I[2] = org[2] + t % T1;
+    } else {
+      I[0] = org[0] + t / T1;
+      I[1] = org[1] + t % T1;
+    }
+    bool in = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) in = in && I[d] < g.R;
+    if (in) sink.add(node_index<DIM>(g.R, I), a, b, c, m);
+  }
+}
+
+template <int DIM, typename T, typename Sink>
+__global__ void __launch_bounds__(kThreads) k_p2g(KParams<T> kp, Geom<DIM> g, PView<T> P,
+                                                  const uint32_t* __restrict__ perm, const int4* __restrict__ chunks,
+                                                  const WsHeader* __restrict__ hdr, Sink sink, int32_t* status,
+                                                  uint32_t* fallbacks) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  T* tile = reinterpret_cast<T*>(smem_raw);
+  const int TN = tile_nodes<DIM>(g);
+  const uint32_t nch = hdr->n_chunks;
+  const uint32_t per = (nch + gridDim.x - 1) / gridDim.x;
+  const uint32_t c0 = blockIdx.x * per;
+  const uint32_t c1 = min(nch, c0 + per);
+  int cur = -1;
+  int org[DIM];
+  for (uint32_t c = c0; c < c1; ++c) {
+    const int4 ch = chunks[c];
+    if (ch.x != cur) {
+      if (cur >= 0) {
+        __syncthreads();
+        p2g_flush<DIM, T, Sink>(tile, TN, g, org, sink);
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < 4 * TN; t += blockDim.x) tile[t] = T(0);
+      cur = ch.x;
+      int bc[DIM];
+      block_coords<DIM>(g, cur, bc);
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) org[d] = bc[d] * g.bs;
+      __syncthreads();
+    }
+    for (int l = threadIdx.x; l < ch.z; l += blockDim.x)
+      p2g_particle<DIM, T>(kp, g, P, perm[ch.y + l], org, tile, TN, status, fallbacks);
+  }
+  if (cur >= 0) {
+    __syncthreads();
+    p2g_flush<DIM, T, Sink>(tile, TN, g, org, sink);
+  }
+}
+
+// ----------------------------------------------------------------------------------------------
+// Grid node rule (three_d/grid_op.py:22-47, two_d/grid_op.py:13-24).  vel holds momentum on
+// entry (or, for the per-phase API, whatever the caller's grid held) and velocity on exit.
+template <int DIM, typename T>
+__device__ __forceinline__ void grid_node(const KParams<T>& kp, const int I[DIM], T vel[3], T m) {
+  if constexpr (DIM == 3) {
+    if (m > T(0)) {
+      vel[0] = vel[0] / m;
+      vel[1] = vel[1] / m;
+      vel[2] = vel[2] / m;
+      vel[1] += kp.dt * kp.gravity;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) vel[d] = ffclamp(vel[d], -kp.v_allowed, kp.v_allowed);
+    }
+    if (kp.wall_mode == FFMPM_WALLS_REFERENCE) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        if (I[d] < 1 || I[d] >= kp.res - 1) vel[d] = T(0);
+    } else {
+      bool near = false;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) near = near || I[d] < 3 || I[d] > kp.res - 3;
+      if (near) vel[0] = vel[1] = vel[2] = T(0);
+    }
+  } else {
+    if (m > T(0)) {
+      vel[0] = vel[0] / m;
+      vel[1] = vel[1] / m;
+      vel[1] += kp.dt * kp.gravity;
+      if (kp.wall_mode == FFMPM_WALLS_REFERENCE) {
+        const double xx = double(I[0]) / double(kp.res), yy = double(I[1]) / double(kp.res);
+        if (xx < 0.05 || xx > 1.0 - 0.05 || yy > 1.0 - 0.05) vel[0] = vel[1] = T(0);
+        if (yy < 0.05) vel[1] = vel[1] > T(0) ? vel[1] : T(0);
+      } else {
+        bool near = I[0] < 3 || I[0] > kp.res - 3 || I[1] < 3 || I[1] > kp.res - 3;
+        if (near) vel[0] = vel[1] = T(0);
+      }
+    }
+    vel[2] = T(0);
+  }
+}
+
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kThreads) k_grid_update(KParams<T> kp, Geom<DIM> g,
+                                                          const uint32_t* __restrict__ touched,
+                                                          const WsHeader* __restrict__ hdr, Node4<T>* __restrict__ A,
+                                                          Node4<T>* __restrict__ B) {
+  const uint32_t nt = hdr->n_touched;
+  const int per_block = DIM == 3 ? g.bs * g.bs * g.bs : g.bs * g.bs;
+  for (uint32_t tb = blockIdx.x; tb < nt; tb += gridDim.x) {
+    int bc[DIM];
+    block_coords<DIM>(g, (int)touched[tb], bc);
+    for (int t = threadIdx.x; t < per_block; t += blockDim.x) {
+      int I[DIM];
+      if constexpr (DIM == 3) {
+        I[0] = bc[0] * g.bs + t / (g.bs * g.bs);
+        I[1] = bc[1] * g.bs + (t / g.bs) % g.bs;
+        I[2] = bc[2] * g.bs + t % g.bs;
+      } else {
+        I[0] = bc[0] * g.bs + t / g.bs;
+        I[1] = bc[1] * g.bs + t % g.bs;
+      }
+      bool in = true;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) in = in && I[d] < g.R;
+      if (!in) continue;
+      const int64_t node = node_index<DIM>(g.R, I);
+      const Node4<T> a = A[node];
+      T vel[3] = {a.x, a.y, a.z};
+      grid_node<DIM, T>(kp, I, vel, a.w);
+      B[node] = Node4<T>{vel[0], vel[1], vel[2], a.w};
+      A[node] = Node4<T>{T(0), T(0), T(0), T(0)};
+    }
+  }
+}
+
+// Dense per-phase grid_op on the caller's arrays (every node, as the reference sweeps).
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kThreads) k_grid_op_dense(KParams<T> kp, int R, T* __restrict__ gv,
+                                                            const T* __restrict__ gm) {
+  const int64_t nn = DIM == 3 ? (int64_t)R * R * R : (int64_t)R * R;
+  for (int64_t node = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; node < nn;
+       node += (int64_t)gridDim.x * blockDim.x) {
+    int I[DIM];
+    if constexpr (DIM == 3) {
+      I[0] = (int)(node / ((int64_t)R * R));
+      I[1] = (int)((node / R) % R);
+      I[2] = (int)(node % R);
+    } else {
+      I[0] = (int)(node / R);
+      I[1] = (int)(node % R);
+    }
+    T vel[3] = {gv[node * DIM + 0], gv[node * DIM + 1], DIM == 3 ? gv[node * DIM + DIM - 1] : T(0)};
+    grid_node<DIM, T>(kp, I, vel, gm[node]);
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) gv[node * DIM + d] = vel[d];
+  }
+}
+
+// ----------------------------------------------------------------------------------------------
+// G2P.  The tile of grid velocities for the chunk's block ((bs+2)^DIM nodes of Node4) is staged in
+// shared memory, either by one TMA bulk-tensor copy from the workspace grid (kTma) or by plain
+// loads from the caller's grid (per-phase API).
+struct G2PExtra {
+  const int32_t* ids_in;
+  int32_t* ids_out;
+  uint32_t* keys_next;    // sorted mode: key of the updated position (next substep's sort input)
+  uint32_t* block_count;  // sorted mode: histogram for the next substep
+  int cell_bits;
+};
+
+template <int DIM, typename T>
+__device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DIM>& g, const PView<T>& Pin,
+                                             const PView<T>& Pout, uint32_t p, uint32_t q, const int org[DIM],
+                                             const Node4<T>* tile, int32_t* status, bool sorted,
+                                             const G2PExtra& ex) {
+  constexpr int DD = DIM * DIM;
+  T xp[DIM], fx[DIM], w[3][DIM];
+  int lb[DIM];
+  bool ok = true;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    xp[d] = Pin.x[(size_t)p * DIM + d];
+    int b;
+    ok = ok && base_of(xp[d], kp.inv_dx, kp.res, b, fx[d]);
+    lb[d] = b - org[d];
+    ok = ok && lb[d] >= 0 && lb[d] + 2 < g.tile;
+    T ww[3];
+    bspline(fx[d], ww);
+    w[0][d] = ww[0];
+    w[1][d] = ww[1];
+    w[2][d] = ww[2];
+  }
+  if (!ok) {
+    raise_status(status, FFMPM_STATUS_OOB);
+    return;
+  }
+  T v[DIM], Cn[DD];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) v[d] = T(0);
+#pragma unroll
+  for (int i = 0; i < DD; ++i) Cn[i] = T(0);
+  const int T1 = g.tile;
+  if constexpr (DIM == 3) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const T d0 = T(i) - fx[0];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const T d1 = T(j) - fx[1];
+        const T wij = w[i][0] * w[j][1];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const T d2 = T(k) - fx[2];
+          const T weight = wij * w[k][2];
+          const Node4<T> gvn = tile[((lb[0] + i) * T1 + (lb[1] + j)) * T1 + (lb[2] + k)];
+          const T wv0 = weight * gvn.x, wv1 = weight * gvn.y, wv2 = weight * gvn.z;
+          v[0] += wv0;
+          v[1] += wv1;
+          v[2] += wv2;
+          Cn[0] += wv0 * d0; Cn[1] += wv0 * d1; Cn[2] += wv0 * d2;
+          Cn[3] += wv1 * d0; Cn[4] += wv1 * d1; Cn[5] += wv1 * d2;
+          Cn[6] += wv2 * d0; Cn[7] += wv2 * d1; Cn[8] += wv2 * d2;
+        }
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const T d0 = T(i) - fx[0];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const T d1 = T(j) - fx[1];
+        const T weight = w[i][0] * w[j][1];
+        const Node4<T> gvn = tile[(lb[0] + i) * T1 + (lb[1] + j)];
+        const T wv0 = weight * gvn.x, wv1 = weight * gvn.y;
+        v[0] += wv0;
+        v[1] += wv1;
+        Cn[0] += wv0 * d0; Cn[1] += wv0 * d1;
+        Cn[2] += wv1 * d0; Cn[3] += wv1 * d1;
+      }
+    }
+  }
+  const T c4 = T(4) * kp.inv_dx;
+#pragma unroll
+  for (int i = 0; i < DD; ++i) Cn[i] *= c4;
+  T F[DD], Fn[DD];
+#pragma unroll
+  for (int i = 0; i < DD; ++i) F[i] = Pin.F[(size_t)p * DD + i];
+  // F <- (I + dt C) F   (g2p.py:46)
+#pragma unroll
+  for (int r = 0; r < DIM; ++r)
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) acc += ((r == k ? T(1) : T(0)) + kp.dt * Cn[r * DIM + k]) * F[k * DIM + c];
+      Fn[r * DIM + c] = acc;
+    }
+  T jp_new = T(1);
+  const bool write_jp = (DIM == 2) || sorted || kp.model == FFMPM_MODEL_SNOW;
+  if (write_jp) jp_new = Pin.Jp[p];
+  if constexpr (DIM == 2) {
+    // two_d/g2p.py:37-46: SVD, clamp (snow only), rebuild, Jp update.  Without the clamp the
+    // rebuild returns F itself (up to the sign convention of the SVD), so only snow rebuilds.
+    const T oldJ = Fn[0] * Fn[3] - Fn[1] * Fn[2];
+    if (kp.model == FFMPM_MODEL_SNOW) {
+      T U[4], s[2], V[4];
+      svd2<T>(Fn, U, s, V);
+      s[0] = ffclamp(s[0], T(1.0 - 2.5e-2), T(1.0 + 7.5e-3));
+      s[1] = ffclamp(s[1], T(1.0 - 2.5e-2), T(1.0 + 7.5e-3));
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) Fn[i * 2 + j] = U[i * 2 + 0] * s[0] * V[j * 2 + 0] + U[i * 2 + 1] * s[1] * V[j * 2 + 1];
+    }
+    const T det = (Fn[0] * Fn[3] - Fn[1] * Fn[2]) + T(1e-10);
+    jp_new = ffclamp(jp_new * oldJ / det, T(0.6), T(20.0));
+  }
+  T xn[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) xn[d] = xp[d] + kp.dt * v[d];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    Pout.x[(size_t)q * DIM + d] = xn[d];
+    Pout.v[(size_t)q * DIM + d] = v[d];
+  }
+#pragma unroll
+  for (int i = 0; i < DD; ++i) {
+    Pout.C[(size_t)q * DD + i] = Cn[i];
+    Pout.F[(size_t)q * DD + i] = Fn[i];
+  }
+  if (write_jp) Pout.Jp[q] = jp_new;
+  if (sorted) {
+    if (Pin.mass) Pout.mass[q] = Pin.mass[p];
+    if (Pin.mu0) Pout.mu0[q] = Pin.mu0[p];
+    if (Pin.lam0) Pout.lam0[q] = Pin.lam0[p];
+    if (ex.ids_in) ex.ids_out[q] = ex.ids_in[p];
+    if (ex.keys_next) {
+      // key of the updated position: the next substep's sort input (fused to avoid re-reading x)
+      uint32_t key, blk;
+      const bool valid = particle_key<DIM, T>(xn, kp, g, ex.cell_bits, key, blk);
+      if (!valid) raise_status(status, FFMPM_STATUS_OOB);
+      ex.keys_next[q] = key;
+      warp_count(ex.block_count, blk, valid);
+    }
+  }
+}
+
+template <int DIM, typename T, bool kTma, bool kSorted>
+__global__ void __launch_bounds__(kThreads) k_g2p(KParams<T> kp, Geom<DIM> g, PView<T> Pin, PView<T> Pout,
+                                                  const uint32_t* __restrict__ perm, const int4* __restrict__ chunks,
+                                                  const WsHeader* __restrict__ hdr, const __grid_constant__ CUtensorMap tmap,
+                                                  const T* __restrict__ user_gv, G2PExtra ex, int32_t* status) {
+  // Dynamic shared memory: [pad to 128 B][tile: TN Node4][mbarrier].  The TMA destination must
+  // be 128-byte aligned, so the tile start is rounded up explicitly.
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int TN = tile_nodes<DIM>(g);
+  const uint32_t pad = (128u - (smem_u32(smem_raw) & 127u)) & 127u;
+  Node4<T>* tile = reinterpret_cast<Node4<T>*>(smem_raw + pad);
+  uint64_t& bar = *reinterpret_cast<uint64_t*>(smem_raw + pad + TN * sizeof(Node4<T>));
+  const uint32_t nch = hdr->n_chunks;
+  const uint32_t per = (nch + gridDim.x - 1) / gridDim.x;
+  const uint32_t c0 = blockIdx.x * per;
+  const uint32_t c1 = min(nch, c0 + per);
+  if constexpr (kTma) {
+    if (threadIdx.x == 0) {
+      mbar_init(&bar, 1);
+      fence_barrier_init();
+    }
+    __syncthreads();
+  }
+  uint32_t phase = 0;
+  int cur = -1;
+  int org[DIM];
+  bool timed_out = false;
+  for (uint32_t c = c0; c < c1; ++c) {
+    const int4 ch = chunks[c];
+    if (ch.x != cur) {
+      __syncthreads();  // every thread is done with the previous tile
+      cur = ch.x;
+      int bc[DIM];
+      block_coords<DIM>(g, cur, bc);
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) org[d] = bc[d] * g.bs;
+      if constexpr (kTma) {
+        if (threadIdx.x == 0) {
+          const uint32_t bytes = (uint32_t)(TN * sizeof(Node4<T>));
+          mbar_arrive_expect_tx(&bar, bytes);
+          if constexpr (DIM == 3)
+            tma_load_4d(tile, &tmap, &bar, 0, org[2], org[1], org[0]);
+          else
+            tma_load_3d(tile, &tmap, &bar, 0, org[1], org[0]);
+        }
+        if (!mbar_wait(&bar, phase)) {
+          timed_out = true;
+        }
+        phase ^= 1u;
+        if (__syncthreads_or(timed_out)) {
+          raise_status(status, FFMPM_STATUS_TIMEOUT);
+          return;
+        }
+      } else {
+        const int T1 = g.tile;
+        for (int t = threadIdx.x; t < TN; t += blockDim.x) {
+          int I[DIM];
+          if constexpr (DIM == 3) {
+            I[0] = org[0] + t / (T1 * T1);
+            I[1] = org[1] + (t / T1) % T1;
+            I[2] = org[2] + t % T1;
+          } else {
+            I[0] = org[0] + t / T1;
+            I[1] = org[1] + t % T1;
+          }
+          bool in = true;
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) in = in && I[d] < g.R;
+          Node4<T> nv{T(0), T(0), T(0), T(0)};
+          if (in) {
+            const int64_t node = node_index<DIM>(g.R, I);
+            nv.x = user_gv[node * DIM + 0];
+            nv.y = user_gv[node * DIM + 1];
+            if constexpr (DIM == 3) nv.z = user_gv[node * DIM + 2];
+          }
+          tile[t] = nv;
+        }
+        __syncthreads();
+      }
+    }
+    for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {
+      const uint32_t s = ch.y + l;
+      const uint32_t p = perm[s];
+      const uint32_t q = kSorted ? s : p;
+      g2p_particle<DIM, T>(kp, g, Pin, Pout, p, q, org, tile, status, kSorted, ex);
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------------------------
+__global__ void k_diag_init(double* out) {
+  if (threadIdx.x < 8) out[threadIdx.x] = threadIdx.x < 7 ? 0.0 : 1e300;
+}
+
+// Float64 diagnostics: [KE, elastic energy, gravitational energy, px, py, pz, mass, min det F].
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kThreads) k_diag(KParams<T> kp, PView<T> P, uint32_t n, double* out) {
+  constexpr int DD = DIM * DIM;
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  double mindet = 1e300;
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const double m = P.mass ? double(P.mass[p]) : double(kp.mass);
+    const double mu0 = P.mu0 ? double(P.mu0[p]) : double(kp.mu0);
+    const double lam0 = P.lam0 ? double(P.lam0[p]) : double(kp.lam0);
+    const double h = double(kp.hardening);
+    double v2 = 0;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const double vd = double(P.v[(size_t)p * DIM + d]);
+      v2 += vd * vd;
+      acc[3 + d] += m * vd;
+    }
+    acc[0] += 0.5 * m * v2;
+    acc[2] += -double(kp.gravity) * m * double(P.x[(size_t)p * DIM + 1]);
+    acc[6] += m;
+    double F[DD];
+#pragma unroll
+    for (int i = 0; i < DD; ++i) F[i] = double(P.F[(size_t)p * DD + i]);
+    double J, fr = 0;
+    if constexpr (DIM == 3) {
+      double R[9];
+      polar3_newton<double>(F, R, 60);
+      J = det3(F);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) fr += (F[i] - R[i]) * (F[i] - R[i]);
+    } else {
+      double R[4];
+      polar2<double>(F, R);
+      J = F[0] * F[3] - F[1] * F[2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) fr += (F[i] - R[i]) * (F[i] - R[i]);
+    }
+    // fixed-corotated energy density mu|F-R|^2 + lam/2 (J-1)^2, times the particle volume
+    acc[1] += double(kp.volume) * (mu0 * h * fr + 0.5 * lam0 * h * (J - 1.0) * (J - 1.0));
+    mindet = J < mindet ? J : mindet;
+  }
+  __shared__ double red[8][kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    double vsum = acc[k];
+    for (int o = 16; o > 0; o >>= 1) vsum += __shfl_down_sync(0xffffffffu, vsum, o);
+    if (lane == 0) red[k][warp] = vsum;
+  }
+  {
+    double vm = mindet;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double t = __shfl_down_sync(0xffffffffu, vm, o);
+      vm = t < vm ? t : vm;
+    }
+    if (lane == 0) red[7][warp] = vm;
+  }
+  __syncthreads();
+  if (threadIdx.x < 8) {
+    const int k = threadIdx.x;
+    double r = k < 7 ? 0.0 : 1e300;
+    for (int w = 0; w < kThreads / 32; ++w) r = k < 7 ? r + red[k][w] : (red[k][w] < r ? red[k][w] : r);
+    if (k < 7) {
+      atomicAdd(&out[k], r);
+    } else {
+      // float64 atomic min via CAS on the bit pattern
+      unsigned long long* addr = reinterpret_cast<unsigned long long*>(&out[7]);
+      unsigned long long old = *addr, assumed;
+      do {
+        assumed = old;
+        if (__longlong_as_double(assumed) <= r) break;
+        old = atomicCAS(addr, assumed, __double_as_longlong(r));
+      } while (old != assumed);
+    }
+  }
+}
+
+}  // namespace ffmpm

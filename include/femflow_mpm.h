@@ -1,0 +1,150 @@
+/*
+ * femflow_mpm.h — C ABI of the GB300 (sm_103a) MLS-MPM substep.
+ *
+ * Drop-in boundary for FEMFlow's numba solver path (femflow/solvers/mpm).  Every entry point
+ * takes plain device pointers, sizes, a POD parameter block and a CUDA stream (passed as void*,
+ * i.e. a cudaStream_t), launches its kernels on that stream and returns an FFMPM_* code for
+ * host-side problems (bad arguments, launch failures).  Problems that only the kernels can see
+ * (a particle outside the grid — the reference raises RuntimeError there, utils.py:138-150 and
+ * three_d/p2g.py:51-52) are OR-ed into a status word inside the workspace; read it with
+ * ffmpm_status_read after the stream has run.
+ *
+ * No entry point allocates device memory.  Functions that need scratch take a caller-allocated
+ * workspace of ffmpm_workspace_size() bytes that ffmpm_workspace_init() has prepared once.
+ * A workspace is bound to one (params, n) shape and one stream at a time.
+ *
+ * Array layouts (row-major, element type float or double per params.real_bytes):
+ *   x, v        [n][dim]              (reference: particle.pos / x, v)
+ *   F, C        [n][dim][dim]         (reference: F, C)
+ *   Jp          [n]                   (reference: Jp[n][1])
+ *   mass, mu_0, lambda_0  [n] or NULL (reference Particle fields, particle.py:10-27; NULL = scalar
+ *                                      params.mass / mu_0 / lambda_0, as two_d/p2g.py:11-29)
+ *   grid velocity [(res+1)^dim][dim], grid mass [(res+1)^dim]  (reference grid_velocity /
+ *                                      grid_mass, first index = x node)
+ */
+#ifndef FEMFLOW_MPM_H
+#define FEMFLOW_MPM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* return codes */
+#define FFMPM_OK 0
+#define FFMPM_ERR_BADARG 3
+#define FFMPM_ERR_WORKSPACE 4
+#define FFMPM_ERR_CUDA 5
+#define FFMPM_ERR_UNSUPPORTED 7
+
+/* status-word bits (device side, see ffmpm_status_read) */
+#define FFMPM_STATUS_OOB 1       /* particle stencil outside the grid, or non-finite position */
+#define FFMPM_STATUS_NONFINITE 2 /* non-finite value produced in the particle state */
+#define FFMPM_STATUS_TIMEOUT 4   /* a bounded device wait expired (never expected) */
+
+/* material models: reference strings of three_d/p2g.py:57-61 */
+#define FFMPM_MODEL_NEO_HOOKEAN 0 /* "neo_hookean": fixed-corotated stress, constant hardening */
+#define FFMPM_MODEL_SNOW 1        /* "snow": exp hardening in P2G + singular-value clamp in G2P */
+
+/* boundary rules of the grid update */
+#define FFMPM_WALLS_REFERENCE 0 /* 3D: three_d/grid_op.py:38-47;  2D: two_d/grid_op.py:13-24 */
+#define FFMPM_WALLS_STICKY3 1   /* all velocity zeroed within 3 cells of every face */
+
+typedef struct ffmpm_params {
+  int32_t dim;          /* 2 or 3 */
+  int32_t res;          /* grid resolution; nodes per axis = res + 1 */
+  int32_t real_bytes;   /* 4 = float32 arrays and arithmetic, 8 = float64 */
+  int32_t model;        /* FFMPM_MODEL_* */
+  int32_t wall_mode;    /* FFMPM_WALLS_* */
+  int32_t deterministic;/* 1: P2G sums in a fixed order (bit-identical across runs) */
+  int32_t block_size;   /* nodes per block side for work assignment; 0 = default */
+  int32_t reserved;
+  double dx, inv_dx, dt;
+  double gravity;       /* added to the axis-1 (y) grid velocity, as the reference */
+  double volume;        /* particle volume (reference argument `volume`) */
+  double hardening;     /* reference argument `hardening` */
+  double mass, mu_0, lambda_0; /* scalar material used when the per-particle pointers are NULL */
+} ffmpm_params;
+
+typedef struct ffmpm_particles {
+  int64_t n;
+  void *x, *v, *F, *C, *Jp;
+  const void *mass, *mu_0, *lambda_0;
+} ffmpm_particles;
+
+typedef struct ffmpm_grid {
+  void *velocity; /* [(res+1)^dim][dim] */
+  void *mass;     /* [(res+1)^dim] */
+} ffmpm_grid;
+
+/* Bytes of workspace needed for `n` particles with these params. */
+int ffmpm_workspace_size(const ffmpm_params *p, int64_t n, size_t *bytes);
+
+/* Prepare a freshly allocated workspace (zeroes its grids and counters).  Call once. */
+int ffmpm_workspace_init(const ffmpm_params *p, int64_t n, void *ws, size_t ws_bytes, void *stream);
+
+/* Synchronise `stream`, then copy out the status word (FFMPM_STATUS_* bits) and the number of
+ * particles whose polar decomposition was redone in float64. */
+int ffmpm_status_read(void *ws, int32_t *status, uint32_t *polar_fallbacks, void *stream);
+int ffmpm_status_clear(void *ws, void *stream);
+
+/* three_d.p2g / two_d.p2g (three_d/p2g.py:14-80, two_d/p2g.py:11-76): scatter the particles'
+ * momentum and mass, ADDING into the caller's grid. */
+int ffmpm_p2g(const ffmpm_params *p, const ffmpm_particles *P, ffmpm_grid *grid, void *ws, size_t ws_bytes,
+              void *stream);
+
+/* three_d.grid_op / two_d.grid_op (three_d/grid_op.py:5-47, two_d/grid_op.py:5-24), in place. */
+int ffmpm_grid_op(const ffmpm_params *p, ffmpm_grid *grid, void *stream);
+
+/* three_d.g2p / two_d.g2p (three_d/g2p.py:9-59, two_d/g2p.py:5-47): gather from the caller's
+ * grid and update x, v, C, F (and Jp) in place. */
+int ffmpm_g2p(const ffmpm_params *p, const ffmpm_grid *grid, ffmpm_particles *P, void *ws, size_t ws_bytes,
+              void *stream);
+
+/* solve_mls_mpm_3d (mls_mpm.py:40-79) and its 2D analogue: one full substep on the caller's
+ * arrays, in place, particle order preserved.  The grid lives in the workspace. */
+int ffmpm_substep(const ffmpm_params *p, ffmpm_particles *P, void *ws, size_t ws_bytes, void *stream);
+
+/* `nsteps` substeps that keep the particles physically sorted by grid block: step k reads
+ * buffer (k even ? a : b) and writes the other one in sorted order, carrying the particle ids
+ * (ids_a/ids_b) along.  After the call the state is in `a` when nsteps is even, else in `b`.
+ * Same arithmetic as ffmpm_substep (MPMSimulation._simulate_offline, simulation.py:122-142). */
+int ffmpm_substeps_sorted(const ffmpm_params *p, ffmpm_particles *a, ffmpm_particles *b, int32_t *ids_a,
+                          int32_t *ids_b, int32_t nsteps, void *ws, size_t ws_bytes, void *stream);
+
+/* Stable radix sort of the particles by grid-block key (the key of each particle's base node):
+ * keys_out[i] is the i-th smallest key, perm_out[i] the index of that particle.  Particles
+ * outside the grid get key 0xFFFFFFFF and sort last.  No reference counterpart: it replaces the
+ * reference's unordered particle loop (three_d/p2g.py:49). */
+int ffmpm_sort_by_block(const ffmpm_params *p, const void *x, int64_t n, uint32_t *keys_out, uint32_t *perm_out,
+                        void *ws, size_t ws_bytes, void *stream);
+
+/* Float64 diagnostics of a particle state, written to device memory `out` (8 doubles):
+ * [kinetic energy, elastic (fixed-corotated) energy, gravitational energy (-g*y*m),
+ *  momentum x, y, z, total mass, min det F].  No reference counterpart. */
+int ffmpm_diagnostics_fp64(const ffmpm_params *p, const ffmpm_particles *P, double *out, void *stream);
+
+/* Same as ffmpm_substeps_sorted, with CUDA events recorded around each phase on `stream`; the
+ * call synchronises the stream and ADDS the per-phase milliseconds and launch counts into
+ * phase_ms[FFMPM_NPHASES] / phase_launches[FFMPM_NPHASES] (host arrays).  Phases: 0 keys,
+ * 1 sort, 2 plan, 3 P2G, 4 grid update, 5 G2P.  No reference counterpart (measurement only). */
+#define FFMPM_NPHASES 6
+int ffmpm_profile_substeps(const ffmpm_params *p, ffmpm_particles *a, ffmpm_particles *b, int32_t *ids_a,
+                           int32_t *ids_b, int32_t nsteps, void *ws, size_t ws_bytes, void *stream,
+                           double *phase_ms, int64_t *phase_launches);
+
+/* Host-only description of the work decomposition for (params, n): info[0] block side, [1] blocks
+ * per axis, [2] blocks, [3] key bits, [4] radix passes, [5] kernels per sorted substep, [6] tile
+ * side, [7] max work chunks.  No reference counterpart. */
+int ffmpm_plan_info(const ffmpm_params *p, int64_t n, int64_t *info);
+
+/* Library version string. */
+const char *ffmpm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FEMFLOW_MPM_H */

@@ -1,0 +1,130 @@
+"""Block sort bit-exactness, the resident sorted solver, CUDA-graph replay and FP64 diagnostics."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_helpers import close, n, t
+from femflow_gb300 import _native as N
+from femflow_gb300 import engine as E
+from femflow_gb300.solver import MPMSolver
+from femflow_gb300.solvers.mpm import mls_mpm
+from femflow_gb300.solvers.mpm.particle import ParticleSet
+from test_gpu_parity_3d import two_cubes
+
+pytestmark = pytest.mark.gpu
+
+
+def host_keys(x32, res, bs, det):
+    """Block keys computed on the host with the kernels' rounding (float32 mul, then sub)."""
+    xs = (x32 * np.float32(res)).astype(np.float32)
+    tt = (xs - np.float32(0.5)).astype(np.float32)
+    valid = np.all((tt > -1) & (tt < res), axis=1)
+    b = np.where(valid[:, None], np.trunc(tt), 0).astype(np.int64)
+    valid &= np.all((b >= 0) & (b + 2 <= res), axis=1)
+    R = res + 1
+    nb = (R + bs - 1) // bs
+    blk = np.zeros(len(x32), dtype=np.int64)
+    cell = np.zeros(len(x32), dtype=np.int64)
+    for dd in range(x32.shape[1]):
+        blk = blk * nb + b[:, dd] // bs
+        cell = cell * bs + b[:, dd] % bs
+    cbits = x32.shape[1] * int(np.log2(bs)) if det else 0
+    key = (blk << cbits) | cell if det else blk
+    key = np.where(valid, key, 0xFFFFFFFF).astype(np.uint64)
+    return key
+
+
+@pytest.mark.parametrize("dim,res,det", [(3, 64, False), (3, 128, False), (3, 64, True), (2, 128, False), (2, 256, True)])
+def test_sort_by_block_is_bit_exact_stable(dim, res, det):
+    rng = np.random.default_rng(7)
+    nn = 200_003
+    x = rng.uniform(0.05, 0.95, size=(nn, dim)).astype(np.float32)
+    x[::997] = 1.5  # out of the grid: key 0xFFFFFFFF, sorted last
+    prm = E.make_params(dim, res, torch.float32, 1 / res, float(res), 1e-4, deterministic=det)
+    ws = E.Workspace(prm, nn, "cuda")
+    xd = torch.from_numpy(x).cuda()
+    keys = torch.empty(nn, dtype=torch.int32, device="cuda")
+    perm = torch.empty(nn, dtype=torch.int32, device="cuda")
+    N.call("ffmpm_sort_by_block", ctypes.byref(prm), ctypes.c_void_p(xd.data_ptr()), nn,
+           ctypes.c_void_p(keys.data_ptr()), ctypes.c_void_p(perm.data_ptr()), ctypes.c_void_p(ws.ptr),
+           ctypes.c_size_t(ws.bytes), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    bs = (8 if not det else 4) if dim == 3 else (16 if not det else 8)
+    hk = host_keys(x, res, bs, det)
+    ref_perm = np.argsort(hk, kind="stable")
+    got_keys = keys.cpu().numpy().view(np.uint32).astype(np.uint64)
+    assert np.array_equal(got_keys, hk[ref_perm])
+    assert np.array_equal(perm.cpu().numpy().astype(np.int64), ref_perm)
+    st, _ = ws.status()
+    assert st & N.STATUS_OOB  # the planted out-of-grid particles are reported
+
+
+def _scene(dtype, n_per=3000, res=32):
+    s = two_cubes(n_per, res)
+    return s
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_sorted_solver_matches_in_place_substeps(dtype):
+    s = _scene(dtype)
+    res, dt, g, steps = s["res"], 2e-4, -9.8, 10
+    solver = MPMSolver(torch.tensor(s["x"]), res=res, dt=dt, gravity=g, volume=s["vol"],
+                       mass=torch.tensor(s["mass"]), mu_0=torch.tensor(s["mu"]), lambda_0=torch.tensor(s["lam"]),
+                       v=torch.tensor(s["v"]), dtype=dtype)
+    solver.step(steps, check=True)
+    got = solver.state()
+    N_ = len(s["x"])
+    ps = ParticleSet(t(s["x"], dtype), t(s["mass"], dtype), t(s["mu"], dtype), t(s["lam"], dtype))
+    v, F, C, Jp = mls_mpm.make_mls_mpm_coefficients(N_, 3, dtype=dtype)
+    v.copy_(t(s["v"], dtype))
+    for _ in range(steps):
+        mls_mpm.solve_mls_mpm_3d(res, float(res), 1.0, 1 / res, dt, s["vol"], g, ps, v, F, C, Jp)
+    rel = 1e-12 if dtype == torch.float64 else 1e-5
+    close(n(got["x"]), n(ps.pos), rel, scale=1.0, what="x")
+    close(n(got["v"]), n(v), 50 * rel, scale=1.0, what="v")
+    close(n(got["F"]), n(F), 10 * rel, scale=1.0, what="F")
+    # the ids are a permutation and the state stays sorted by block
+    ids = solver.sorted_state()["ids"].cpu().numpy()
+    assert np.array_equal(np.sort(ids), np.arange(N_))
+
+
+def test_graph_replay_matches_direct_launches():
+    s = _scene(torch.float64)
+    kw = dict(res=s["res"], dt=2e-4, gravity=-9.8, volume=s["vol"], mass=torch.tensor(s["mass"]),
+              mu_0=torch.tensor(s["mu"]), lambda_0=torch.tensor(s["lam"]), v=torch.tensor(s["v"]),
+              dtype=torch.float64)
+    a = MPMSolver(torch.tensor(s["x"]), **kw)
+    b = MPMSolver(torch.tensor(s["x"]), **kw)
+    a.step(2)  # graph capture warms up with 2 direct substeps
+    a.capture(4)
+    a.step(8)
+    b.step(10)
+    close(n(a.state()["x"]), n(b.state()["x"]), 1e-12, scale=1.0, what="x graph vs direct")
+    a.check()
+
+
+def test_fp64_diagnostics_match_numpy():
+    s = _scene(torch.float32, n_per=1000)
+    solver = MPMSolver(torch.tensor(s["x"]), res=s["res"], dt=2e-4, gravity=-9.8, volume=s["vol"],
+                       mass=torch.tensor(s["mass"]), mu_0=torch.tensor(s["mu"]), lambda_0=torch.tensor(s["lam"]),
+                       v=torch.tensor(s["v"]), dtype=torch.float32)
+    solver.step(6)
+    d = solver.diagnostics()
+    st = solver.sorted_state()
+    m = st["mass"].double().cpu().numpy()
+    vv = st["v"].double().cpu().numpy()
+    xx = st["x"].double().cpu().numpy()
+    F = st["F"].double().cpu().numpy()
+    assert np.isclose(d["kinetic"], 0.5 * (m * (vv ** 2).sum(1)).sum(), rtol=1e-12)
+    assert np.allclose(d["momentum"], (m[:, None] * vv).sum(0), rtol=1e-12, atol=1e-15)
+    assert np.isclose(d["mass"], m.sum(), rtol=1e-12)
+    assert np.isclose(d["gravitational"], (9.8 * m * xx[:, 1]).sum(), rtol=1e-12)
+    assert np.isclose(d["min_det_F"], np.linalg.det(F).min(), rtol=1e-9)
+    U, sig, Vt = np.linalg.svd(F)
+    R = U @ Vt
+    mu = st["mu_0"].double().cpu().numpy(); lam = st["lambda_0"].double().cpu().numpy()
+    J = np.linalg.det(F)
+    el = (s["vol"] * (mu * ((F - R) ** 2).sum((1, 2)) + 0.5 * lam * (J - 1) ** 2)).sum()
+    assert np.isclose(d["elastic"], el, rtol=1e-8)

@@ -1,0 +1,53 @@
+"""Host-side pieces that need no GPU: parameter packing, particle containers, helpers."""
+import numpy as np
+import pytest
+import torch
+
+from femflow_gb300 import _native as N
+from femflow_gb300 import engine as E
+from femflow_gb300.solvers.mpm import particle as PT
+from femflow_gb300.solvers.mpm import utils as U
+
+
+def test_params_packing():
+    p = E.make_params(3, 64, torch.float64, 1 / 64, 64.0, 1e-4, -9.8, 2e-6, 1.0, model="snow", wall_mode="sticky3")
+    assert (p.dim, p.res, p.real_bytes, p.model, p.wall_mode) == (3, 64, 8, 1, 1)
+    assert p.gravity == -9.8 and p.volume == 2e-6
+    with pytest.raises(TypeError):
+        E.make_params(3, 64, torch.int32, 1, 1, 1)
+
+
+def test_particle_set_roundtrip():
+    ps = [PT.Particle(np.array([0.1, 0.2, 0.3]), 0.0, 2.0, 3.0, 4.0), PT.Particle(np.array([0.4, 0.5, 0.6]), 0.0, 1.0, 1.0, 1.0)]
+    s = PT.ParticleSet.from_particles(ps)
+    assert s.pos.shape == (2, 3) and s.mass.tolist() == [2.0, 1.0]
+    assert s.lambda_0.tolist() == [3.0, 1.0] and s.mu_0.tolist() == [4.0, 1.0]  # Particle(pos, force, mass, lambda_, mu)
+    s.pos += 1.0
+    s.write_positions(ps)
+    assert np.allclose(ps[0].pos, [1.1, 1.2, 1.3])
+    np.testing.assert_allclose(PT.map_particles_to_pos(ps, 2.0), np.array([[1.1, 1.2, 1.3], [1.4, 1.5, 1.6]]).reshape(-1) / 2)
+
+
+def test_particle_set_length_mismatch():
+    with pytest.raises(ValueError):
+        PT.ParticleSet(torch.zeros(3, 3), torch.zeros(2), torch.zeros(3), torch.zeros(3))
+
+
+def test_utils_match_reference_formulas():
+    assert U.constant_hardening(2.0, 3.0, 10.0) == (20.0, 30.0)
+    mu, lam = U.snow_hardening(2.0, 3.0, 10.0, np.array([0.9]))
+    assert np.isclose(mu, 2.0 * np.exp(1.0)) and np.isclose(lam, 3.0 * np.exp(1.0))
+    assert U.oob(np.array([0, 0, 127]), 129, np.array([0, 0, 2]))
+    assert not U.oob(np.array([0, 0, 126]), 129, np.array([0, 0, 2]))
+    assert np.isclose(U.Ev_to_mu(1e4, 0.2), 4166.666666666667)
+    assert np.isclose(U.Ev_to_lambda(1e4, 0.2), 2777.777777777778)
+
+
+def test_no_cpu_fallback_without_gpu():
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    from femflow_gb300.solvers.mpm import mls_mpm
+    v, F, C, Jp = mls_mpm.make_mls_mpm_coefficients(4, 3, device="cpu")
+    ps = PT.ParticleSet(torch.rand(4, 3) * 0.5 + 0.25, torch.ones(4), torch.ones(4), torch.ones(4))
+    with pytest.raises(RuntimeError, match="CUDA"):
+        mls_mpm.solve_mls_mpm_3d(16, 16.0, 1.0, 1 / 16, 1e-4, 1.0, -9.8, ps, v, F, C, Jp)
