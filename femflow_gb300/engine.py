@@ -150,10 +150,15 @@ def stage(arrays, device=None, dtype=None) -> Staged:
         else:
             t = a
             host.append(a if not a.is_cuda else None)
-        if not t.is_cuda:
+        if t.is_cuda:
+            if dtype is not None and t.dtype != dtype:
+                raise TypeError(f"all arrays must share one dtype ({dtype}), got {t.dtype}")
+            if not t.is_contiguous():
+                raise TypeError("CUDA arrays are updated in place and must be contiguous")
+        else:
             t = t.to(device, non_blocking=True)
-        if dtype is not None and t.dtype != dtype:
-            t = t.to(dtype)
+            if dtype is not None and t.dtype != dtype:
+                t = t.to(dtype)
         if not t.is_contiguous():
             t = t.contiguous()
         dev.append(t)

@@ -97,8 +97,7 @@ def test_graph_replay_matches_direct_launches():
               dtype=torch.float64)
     a = MPMSolver(torch.tensor(s["x"]), **kw)
     b = MPMSolver(torch.tensor(s["x"]), **kw)
-    a.step(2)  # graph capture warms up with 2 direct substeps
-    a.capture(4)
+    a.capture(4)  # runs 2 direct warm-up substeps before capturing
     a.step(8)
     b.step(10)
     close(n(a.state()["x"]), n(b.state()["x"]), 1e-12, scale=1.0, what="x graph vs direct")
