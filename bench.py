@@ -44,17 +44,9 @@ WORKLOAD = "two_cubes_1M_res128"
 
 
 def scene(seed: int = 0):
-    rng = np.random.default_rng(seed)
-    a = rng.uniform(-EDGE / 2, EDGE / 2, (N_PER_CUBE, 3)) + np.array([0.35, 0.5, 0.5])
-    b = rng.uniform(-EDGE / 2, EDGE / 2, (N_PER_CUBE, 3)) + np.array([0.65, 0.5, 0.5])
-    x = np.concatenate([a, b])
-    n = len(x)
-    v = np.zeros((n, 3))
-    v[:N_PER_CUBE, 0], v[N_PER_CUBE:, 0] = 1.0, -1.0
-    vol = 2 * EDGE ** 3 / n
-    mu = E_YOUNG / (2 * (1 + NU))
-    lam = E_YOUNG * NU / ((1 + NU) * (1 - 2 * NU))
-    return dict(x=x, v=v, n=n, vol=vol, mass=vol, mu=mu, lam=lam)
+    from femflow_gb300.scenes import two_cubes
+
+    return two_cubes(N_PER_CUBE, edge=EDGE, speed=1.0, E=E_YOUNG, nu=NU, seed=seed)
 
 
 def config(extra=None):
