@@ -20,8 +20,10 @@ ERR_BADARG = 3
 ERR_WORKSPACE = 4
 ERR_CUDA = 5
 ERR_UNSUPPORTED = 7
+ERR_CAPACITY = 8
 ERRORS = {ERR_BADARG: "bad argument", ERR_WORKSPACE: "workspace too small or misaligned", ERR_CUDA: "CUDA error",
-          ERR_UNSUPPORTED: "unsupported configuration"}
+          ERR_UNSUPPORTED: "unsupported configuration", ERR_CAPACITY: "more particles than the static scratch holds"}
+STATIC_SORT_MAX_N = 262144
 
 STATUS_OOB = 1
 STATUS_NONFINITE = 2
@@ -75,6 +77,7 @@ _PROTOS = {
     "ffmpm_profile_substeps": (ctypes.c_int, [_P(Params), _P(Particles), _P(Particles), _vp, _vp, ctypes.c_int32,
                                               _vp, ctypes.c_size_t, _vp, _P(ctypes.c_double), _P(ctypes.c_int64)]),
     "ffmpm_plan_info": (ctypes.c_int, [_P(Params), ctypes.c_int64, _P(ctypes.c_int64)]),
+    "ffmpm_sort_by_block_static": (ctypes.c_int, [_P(Params), _vp, ctypes.c_int64, _vp, _vp, _vp]),
     "ffmpm_version": (ctypes.c_char_p, []),
 }
 

@@ -754,7 +754,7 @@ __global__ void __launch_bounds__(kThreads) k_g2p(KParams<T> kp, Geom<DIM> g, PV
 }
 
 // ----------------------------------------------------------------------------------------------
-__global__ void k_diag_init(double* out) {
+static __global__ void k_diag_init(double* out) {
   if (threadIdx.x < 8) out[threadIdx.x] = threadIdx.x < 7 ? 0.0 : 1e300;
 }
 

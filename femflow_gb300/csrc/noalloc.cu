@@ -1,0 +1,103 @@
+// ffmpm_sort_by_block_static: the block sort for callers that cannot allocate device memory.
+//
+// The scratch of the sort lives in one file-scope __device__ array of fixed size.  Host code
+// never passes the array's name to a kernel (on the host it is only a stand-in symbol): on the
+// first call on each device, with that device current, cudaGetSymbolAddress gives its device
+// address, which is cached per device and passed to the kernels.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "common.cuh"
+#include "internal.h"
+#include "mpm_kernels.cuh"
+
+namespace ffmpm {
+namespace {
+
+constexpr int64_t kStaticMaxN = FFMPM_STATIC_SORT_MAX_N;
+constexpr int64_t kStaticTiles = (kStaticMaxN + kRadixTile - 1) / kRadixTile;
+// [status word + pad: 64 words][keys_next][keys0][keys1][vals0][vals1][histograms 256 x tiles]
+constexpr size_t kHeaderWords = 64;
+constexpr size_t kStaticWords = kHeaderWords + 5 * size_t(kStaticMaxN) + 256 * size_t(kStaticTiles);
+
+__device__ __align__(256) uint32_t g_sort_scratch[kStaticWords];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+uint32_t* g_scratch[kMaxDevices] = {};
+
+// Device address of g_sort_scratch on the current device (looked up once per device).
+int scratch_on_current_device(uint32_t** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return FFMPM_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_scratch[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_sort_scratch) != cudaSuccess || !p) return FFMPM_ERR_CUDA;
+    g_scratch[dev] = static_cast<uint32_t*>(p);
+  }
+  *out = g_scratch[dev];
+  return FFMPM_OK;
+}
+
+template <int DIM, typename T>
+void sort_static(const ffmpm_params& p, const Layout& L, uint32_t* base, const void* x, uint32_t* keys_out,
+                 uint32_t* perm_out, cudaStream_t s) {
+  KParams<T> kp{};
+  kp.inv_dx = T(p.inv_dx);
+  kp.res = p.res;
+  Geom<DIM> g;
+  g.res = L.res;
+  g.R = L.R;
+  g.bs = L.bs;
+  g.nb = L.nb;
+  g.nblocks = (int)L.nblocks;
+  g.tile = L.tile;
+  const uint32_t n = (uint32_t)L.n;
+  int32_t* status = reinterpret_cast<int32_t*>(base);
+  uint32_t* keys_next = base + kHeaderWords;
+  uint32_t* keys0 = keys_next + kStaticMaxN;
+  uint32_t* keys1 = keys0 + kStaticMaxN;
+  uint32_t* vals0 = keys1 + kStaticMaxN;
+  uint32_t* vals1 = vals0 + kStaticMaxN;
+  uint32_t* hist = vals1 + kStaticMaxN;
+  // the array keeps the previous call's status word: start from zero
+  cudaMemsetAsync(status, 0, sizeof(int32_t), s);
+  k_keys<DIM, T><<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kp, g, static_cast<const T*>(x), n, L.cell_bits,
+                                                                     keys_next, nullptr, status);
+  const uint32_t *ks = nullptr, *perm = nullptr;
+  radix_sort(keys_next, n, L.passes, keys0, keys1, vals0, vals1, hist, (int)L.ntiles, s, &ks, &perm);
+  if (keys_out) cudaMemcpyAsync(keys_out, ks, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
+  if (perm_out) cudaMemcpyAsync(perm_out, perm, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
+}
+
+}  // namespace
+}  // namespace ffmpm
+
+extern "C" int ffmpm_sort_by_block_static(const ffmpm_params* p, const void* x, int64_t n, uint32_t* keys_out,
+                                          uint32_t* perm_out, void* stream) {
+  using namespace ffmpm;
+  if (n > kStaticMaxN) return FFMPM_ERR_CAPACITY;
+  Layout L;
+  if (!p || !make_layout(*p, n, &L)) return FFMPM_ERR_BADARG;
+  if (L.ntiles > kStaticTiles) return FFMPM_ERR_CAPACITY;
+  if (n == 0) return FFMPM_OK;
+  if (!x) return FFMPM_ERR_BADARG;
+  uint32_t* base = nullptr;
+  int rc = scratch_on_current_device(&base);
+  if (rc != FFMPM_OK) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->dim == 3) {
+    if (p->real_bytes == 4)
+      sort_static<3, float>(*p, L, base, x, keys_out, perm_out, s);
+    else
+      sort_static<3, double>(*p, L, base, x, keys_out, perm_out, s);
+  } else {
+    if (p->real_bytes == 4)
+      sort_static<2, float>(*p, L, base, x, keys_out, perm_out, s);
+    else
+      sort_static<2, double>(*p, L, base, x, keys_out, perm_out, s);
+  }
+  return cudaGetLastError() == cudaSuccess ? FFMPM_OK : FFMPM_ERR_CUDA;
+}

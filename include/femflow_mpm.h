@@ -140,6 +140,26 @@ int ffmpm_profile_substeps(const ffmpm_params *p, ffmpm_particles *a, ffmpm_part
  * side, [7] max work chunks.  No reference counterpart. */
 int ffmpm_plan_info(const ffmpm_params *p, int64_t n, int64_t *info);
 
+/* Largest n accepted by ffmpm_sort_by_block_static, and its error when n is larger. */
+#define FFMPM_STATIC_SORT_MAX_N 262144
+#define FFMPM_ERR_CAPACITY 8
+
+/* The block sort of ffmpm_sort_by_block (same keys, same stable permutation) without a workspace
+ * and without any device allocation.  It is meant for callers that cannot allocate device memory:
+ * a host application that owns every GPU allocation and hands its plugins device pointers only,
+ * or a real-time loop that forbids allocation once it has started.  The scratch (about 5.3 MB:
+ * five n-sized key/index arrays plus the digit histograms) is one static array in this library,
+ * which every GPU that loads the library keeps until the process exits.
+ *   - n must be <= FFMPM_STATIC_SORT_MAX_N, otherwise FFMPM_ERR_CAPACITY and nothing runs.
+ *   - The first call on a device looks up the array's device address on the current device
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - Every call uses the same array, which keeps the previous call's contents: two calls whose
+ *     work overlaps on the GPU (different streams or host threads) race and corrupt each other's
+ *     results, so serialise them.
+ * No counterpart in the reference. */
+int ffmpm_sort_by_block_static(const ffmpm_params *p, const void *x, int64_t n, uint32_t *keys_out,
+                               uint32_t *perm_out, void *stream);
+
 /* Library version string. */
 const char *ffmpm_version(void);
 
