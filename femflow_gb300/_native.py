@@ -39,7 +39,7 @@ class Params(ctypes.Structure):
     _fields_ = [
         ("dim", ctypes.c_int32), ("res", ctypes.c_int32), ("real_bytes", ctypes.c_int32), ("model", ctypes.c_int32),
         ("wall_mode", ctypes.c_int32), ("deterministic", ctypes.c_int32), ("block_size", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("variant", ctypes.c_int32),
         ("dx", ctypes.c_double), ("inv_dx", ctypes.c_double), ("dt", ctypes.c_double), ("gravity", ctypes.c_double),
         ("volume", ctypes.c_double), ("hardening", ctypes.c_double), ("mass", ctypes.c_double),
         ("mu_0", ctypes.c_double), ("lambda_0", ctypes.c_double),

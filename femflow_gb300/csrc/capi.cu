@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <set>
 #include <vector>
@@ -56,10 +57,12 @@ bool make_layout(const ffmpm_params& p, int64_t n, Layout* L) {
   L->tile = L->bs + 2;
   L->nblocks = p.dim == 3 ? int64_t(L->nb) * L->nb * L->nb : int64_t(L->nb) * L->nb;
   L->nnodes = p.dim == 3 ? int64_t(L->R) * L->R * L->R : int64_t(L->R) * L->R;
-  L->cell_bits = p.deterministic ? p.dim * ilog2_ceil(L->bs) : 0;
+  // keys order particles by block, then by cell inside the block
+  L->cell_bits = p.dim * ilog2_ceil(L->bs);
   L->key_bits = ilog2_ceil(L->nblocks) + L->cell_bits;
   if (L->key_bits > 31) return false;
-  L->passes = std::max(1, (L->key_bits + 7) / 8);
+  L->passes = std::max(1, (L->key_bits + kMaxDigitBits - 1) / kMaxDigitBits);
+  L->digit_bits = std::max(1, (L->key_bits + L->passes - 1) / L->passes);
   L->n = n;
   L->ntiles = std::max<int64_t>(1, (n + kRadixTile - 1) / kRadixTile);
   L->max_chunks = (n + kChunk - 1) / kChunk + L->nblocks;
@@ -82,7 +85,7 @@ bool make_layout(const ffmpm_params& p, int64_t n, Layout* L) {
   L->off_keys1 = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
   L->off_vals0 = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
   L->off_vals1 = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
-  L->off_hist = take(sizeof(uint32_t) * 256 * L->ntiles);
+  L->off_hist = take(sizeof(uint32_t) * (size_t(1) << L->digit_bits) * (L->ntiles + L->passes));
   L->off_gridA = take(node_bytes * L->nnodes);
   L->off_gridB = take(node_bytes * L->nnodes);
   L->off_stage = take(p.deterministic ? node_bytes * tile_nodes * L->nblocks : 0);
@@ -150,6 +153,7 @@ KParams<T> kparams(const ffmpm_params& p) {
   k.res = p.res;
   k.model = p.model;
   k.wall_mode = p.wall_mode;
+  k.variant = p.variant;
   return k;
 }
 
@@ -219,6 +223,22 @@ int work_grid(int64_t max_items, int per_sm) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(max_items, cap));
 }
 
+// Resident CTAs per SM of `kernel` at kThreads threads and `smem` dynamic bytes (cached), so the
+// chunk-loop kernels launch exactly one wave.
+template <typename F>
+int resident_per_sm(F* kernel, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, size_t>, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair(reinterpret_cast<const void*>(kernel), smem);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kThreads, smem) != cudaSuccess || nb < 1) nb = 1;
+  cache[key] = nb;
+  return nb;
+}
+
 // Optional per-phase CUDA-event timer of the profiling entry point.
 struct PhaseTimer {
   std::vector<cudaEvent_t> ev;     // pairs (start, stop)
@@ -266,7 +286,7 @@ void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const T*
   }
   const uint32_t* ks = nullptr;
   if (tm) tm->begin(1);
-  radix_sort(w.keys_next, n, L.passes, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, s, &ks, perm);
+  radix_sort(w.keys_next, n, L.passes, L.digit_bits, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, s, &ks, perm);
   if (tm) tm->end(3 * L.passes);
   if (tm) tm->begin(2);
   k_plan<DIM><<<1, 1024, 0, s>>>(g, w.block_count, w.block_start, w.block_cnt, w.chunks, w.touched, w.occupied,
@@ -295,11 +315,23 @@ void set_smem(F* kernel, size_t bytes) {
 template <int DIM, typename T, typename Sink>
 void launch_p2g(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<T>& P, const uint32_t* perm,
                 const Sink& sink, cudaStream_t s) {
-  const size_t smem = tile_smem<DIM, T>(L);
-  auto kern = k_p2g<DIM, T, Sink>;
+  const bool direct = (p.variant & kVariantP2GDirect) != 0;
+  const bool lanes = (p.variant & kVariantP2GLanes) != 0;
+  if (!direct && !lanes) {
+    // default: cell-run P2G (tile + per-particle records + cell ids + run starts)
+    const size_t smem = tile_smem<DIM, T>(L) + size_t(kChunk) * RecLayout<DIM>::kStride * sizeof(T) +
+                        sizeof(int) * (2 * kChunk + 1);
+    auto kern = k_p2g_cells<DIM, T, Sink>;
+    set_smem(kern, smem);
+    kern<<<work_grid(L.max_chunks, resident_per_sm(kern, smem)), kThreads, smem, s>>>(
+        kparams<T>(p), geom<DIM>(L), P, perm, w.chunks, w.hdr, sink, &w.hdr->status, &w.hdr->polar_fallbacks);
+    return;
+  }
+  const size_t smem = direct ? 0 : tile_smem<DIM, T>(L);
+  auto kern = direct ? k_p2g<DIM, T, Sink, true> : k_p2g<DIM, T, Sink, false>;
   set_smem(kern, smem);
-  kern<<<work_grid(L.max_chunks, 4), kThreads, smem, s>>>(kparams<T>(p), geom<DIM>(L), P, perm, w.chunks, w.hdr,
-                                                          sink, &w.hdr->status, &w.hdr->polar_fallbacks);
+  kern<<<work_grid(L.max_chunks, resident_per_sm(kern, smem)), kThreads, smem, s>>>(
+      kparams<T>(p), geom<DIM>(L), P, perm, w.chunks, w.hdr, sink, &w.hdr->status, &w.hdr->polar_fallbacks);
 }
 
 template <int DIM, typename T>
@@ -317,8 +349,8 @@ int launch_g2p(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<
   const size_t smem = tile_smem<DIM, T>(L) + 128 + 16;  // + alignment pad + mbarrier
   auto kern = k_g2p<DIM, T, kTma, kSorted>;
   set_smem(kern, smem);
-  kern<<<work_grid(L.max_chunks, 4), kThreads, smem, s>>>(kparams<T>(p), geom<DIM>(L), Pin, Pout, perm, w.chunks,
-                                                          w.hdr, map, user_gv, ex, &w.hdr->status);
+  kern<<<work_grid(L.max_chunks, resident_per_sm(kern, smem)), kThreads, smem, s>>>(
+      kparams<T>(p), geom<DIM>(L), Pin, Pout, perm, w.chunks, w.hdr, map, user_gv, ex, &w.hdr->status);
   return FFMPM_OK;
 }
 
@@ -405,7 +437,7 @@ int op_sort(const ffmpm_params& p, const Layout& L, const Ws& w, const void* x, 
   k_keys<DIM, T><<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kp, g, static_cast<const T*>(x), n, L.cell_bits,
                                                                      w.keys_next, nullptr, &w.hdr->status);
   const uint32_t *ks = nullptr, *perm = nullptr;
-  radix_sort(w.keys_next, n, L.passes, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, s, &ks, &perm);
+  radix_sort(w.keys_next, n, L.passes, L.digit_bits, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, s, &ks, &perm);
   if (keys_out) cudaMemcpyAsync(keys_out, ks, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
   if (perm_out) cudaMemcpyAsync(perm_out, perm, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
   return check_launch();

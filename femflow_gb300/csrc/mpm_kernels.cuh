@@ -23,8 +23,12 @@ namespace ffmpm {
 template <typename T>
 struct KParams {
   T dx, inv_dx, dt, gravity, volume, hardening, mass, mu0, lam0, v_allowed;
-  int res, model, wall_mode;
+  int res, model, wall_mode, variant;
 };
+
+// Variant flags (ffmpm_params.variant).
+constexpr int kVariantP2GDirect = 1;  // P2G scatters straight to L2 with vector reds (no smem tile)
+constexpr int kVariantP2GLanes = 2;   // P2G lane-per-particle shared-tile atomics (no cell runs)
 
 template <typename T>
 struct PView {
@@ -274,10 +278,39 @@ __device__ __forceinline__ void lame_of(const KParams<T>& kp, const PView<T>& P,
   lam = lam0 * e;
 }
 
-// Scatter one particle into the shared tile (SoA: 4 arrays of TN values).
+// Accumulation targets of one particle's 3^DIM contributions, addressed by node coordinates
+// relative to the block origin.
 template <int DIM, typename T>
+struct TileAdder {  // shared tile, SoA: 4 arrays of TN values
+  T* tile;
+  int TN, T1;
+  __device__ __forceinline__ void add(int li, int lj, int lk, T a, T b, T c, T m) const {
+    const int idx = DIM == 3 ? (li * T1 + lj) * T1 + lk : li * T1 + lj;
+    atomicAdd(&tile[idx], a);
+    atomicAdd(&tile[TN + idx], b);
+    if constexpr (DIM == 3) atomicAdd(&tile[2 * TN + idx], c);
+    atomicAdd(&tile[3 * TN + idx], m);
+  }
+};
+
+template <int DIM, typename T, typename Sink>
+struct DirectAdder {  // global grid through the sink (one vector red per node)
+  Sink sink;
+  int R;
+  int org[DIM];
+  __device__ __forceinline__ void add(int li, int lj, int lk, T a, T b, T c, T m) const {
+    int I[DIM];
+    I[0] = org[0] + li;
+    I[1] = org[1] + lj;
+    if constexpr (DIM == 3) I[2] = org[2] + lk;
+    sink.add(node_index<DIM>(R, I), a, b, c, m);
+  }
+};
+
+// Scatter one particle: stress, APIC affine, 3^DIM weighted contributions into `acc`.
+template <int DIM, typename T, typename Adder>
 __device__ __forceinline__ void p2g_particle(const KParams<T>& kp, const Geom<DIM>& g, const PView<T>& P, uint32_t p,
-                                             const int org[DIM], T* tile, int TN, int32_t* status,
+                                             const int org[DIM], const Adder& acc, int32_t* status,
                                              uint32_t* fallbacks) {
   constexpr int DD = DIM * DIM;
   T fx[DIM], w[3][DIM];
@@ -315,7 +348,6 @@ __device__ __forceinline__ void p2g_particle(const KParams<T>& kp, const Geom<DI
 #pragma unroll
   for (int d = 0; d < DIM; ++d) mv[d] = v[d] * m;
   if constexpr (DIM == 3) {
-    const int T1 = g.tile;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       const T d0 = (T(i) - fx[0]) * dx;
@@ -327,16 +359,13 @@ __device__ __forceinline__ void p2g_particle(const KParams<T>& kp, const Geom<DI
         for (int k = 0; k < 3; ++k) {
           const T d2 = (T(k) - fx[2]) * dx;
           const T weight = wij * w[k][2];
-          const int idx = ((lb[0] + i) * T1 + (lb[1] + j)) * T1 + (lb[2] + k);
-          atomicAdd(&tile[idx], weight * (mv[0] + (A[0] * d0 + A[1] * d1 + A[2] * d2)));
-          atomicAdd(&tile[TN + idx], weight * (mv[1] + (A[3] * d0 + A[4] * d1 + A[5] * d2)));
-          atomicAdd(&tile[2 * TN + idx], weight * (mv[2] + (A[6] * d0 + A[7] * d1 + A[8] * d2)));
-          atomicAdd(&tile[3 * TN + idx], weight * m);
+          acc.add(lb[0] + i, lb[1] + j, lb[2] + k, weight * (mv[0] + (A[0] * d0 + A[1] * d1 + A[2] * d2)),
+                  weight * (mv[1] + (A[3] * d0 + A[4] * d1 + A[5] * d2)),
+                  weight * (mv[2] + (A[6] * d0 + A[7] * d1 + A[8] * d2)), weight * m);
         }
       }
     }
   } else {
-    const int T1 = g.tile;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       const T d0 = (T(i) - fx[0]) * dx;
@@ -344,10 +373,8 @@ __device__ __forceinline__ void p2g_particle(const KParams<T>& kp, const Geom<DI
       for (int j = 0; j < 3; ++j) {
         const T d1 = (T(j) - fx[1]) * dx;
         const T weight = w[i][0] * w[j][1];
-        const int idx = (lb[0] + i) * T1 + (lb[1] + j);
-        atomicAdd(&tile[idx], weight * (mv[0] + (A[0] * d0 + A[1] * d1)));
-        atomicAdd(&tile[TN + idx], weight * (mv[1] + (A[2] * d0 + A[3] * d1)));
-        atomicAdd(&tile[3 * TN + idx], weight * m);
+        acc.add(lb[0] + i, lb[1] + j, 0, weight * (mv[0] + (A[0] * d0 + A[1] * d1)),
+                weight * (mv[1] + (A[2] * d0 + A[3] * d1)), T(0), weight * m);
       }
     }
   }
@@ -376,7 +403,237 @@ __device__ __forceinline__ void p2g_flush(const T* tile, int TN, const Geom<DIM>
   }
 }
 
+// ----------------------------------------------------------------------------------------------
+// Cell-run P2G.  Particles arrive sorted by cell inside their block, so a chunk holds runs of
+// particles that share a base cell and therefore all 3^DIM stencil nodes.  Phase 1 (one thread per
+// particle) computes each particle's record once.  Phase 2 finds the runs.  Phase 3 gives each run
+// to a warp whose lanes are the stencil nodes: every lane sums its node's contributions over the
+// run's particles in registers and adds the sum to the shared tile once, so the tile sees one
+// atomic per (node, run) instead of one per (node, particle).
+//
+// Record (floats): [m, q (DIM), a = dx A (DIM^2, row-major), wx0..2, wy0..2 (, wz0..2)] with
+// q = m v - dx A fx; the contribution to node o is w_o (q + a o, m), algebraically the reference's
+// w (m v + A (o - fx) dx, m).
+template <int DIM>
+struct RecLayout {
+  static constexpr int kFloats = DIM == 3 ? 22 : 13;  // m, q (DIM), dx A (DIM^2), weights (3 DIM)
+  static constexpr int kStride = DIM == 3 ? 25 : 13;  // odd: the per-thread stores hit distinct banks
+  static_assert(kFloats == 1 + DIM + DIM * DIM + 3 * DIM, "record size");
+  static constexpr int kW = DIM == 3 ? 13 : 7;        // first weight
+};
+
+template <int DIM, typename T>
+__device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>& g, const PView<T>& P, uint32_t p,
+                                           const int org[DIM], T* rec, int& cell, int32_t* status,
+                                           uint32_t* fallbacks) {
+  constexpr int DD = DIM * DIM;
+  T fx[DIM], w[3][DIM];
+  int lb[DIM];
+  bool ok = true;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    int b;
+    ok = ok && base_of(P.x[(size_t)p * DIM + d], kp.inv_dx, kp.res, b, fx[d]);
+    lb[d] = b - org[d];
+    ok = ok && lb[d] >= 0 && lb[d] + 2 < g.tile;
+    T ww[3];
+    bspline(fx[d], ww);
+    w[0][d] = ww[0];
+    w[1][d] = ww[1];
+    w[2][d] = ww[2];
+  }
+  if (!ok) {
+    raise_status(status, FFMPM_STATUS_OOB);
+    return false;
+  }
+  cell = DIM == 3 ? (lb[0] * g.bs + lb[1]) * g.bs + lb[2] : lb[0] * g.bs + lb[1];
+  T m, mu, lam;
+  lame_of(kp, P, p, m, mu, lam);
+  T F[DD], C[DD], A[DD], v[DIM];
+#pragma unroll
+  for (int i = 0; i < DD; ++i) {
+    F[i] = P.F[(size_t)p * DD + i];
+    C[i] = P.C[(size_t)p * DD + i];
+  }
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) v[d] = P.v[(size_t)p * DIM + d];
+  affine_of<DIM, T>(kp, F, C, m, mu, lam, A, fallbacks);
+  const T dx = kp.dx;
+  rec[0] = m;
+#pragma unroll
+  for (int r = 0; r < DIM; ++r) {
+    T af = T(0);
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) af += A[r * DIM + c] * fx[c];
+    rec[1 + r] = v[r] * m - dx * af;
+  }
+  constexpr int a0 = DIM == 3 ? 4 : 3;
+#pragma unroll
+  for (int i = 0; i < DD; ++i) rec[a0 + i] = dx * A[i];
+  constexpr int w0 = RecLayout<DIM>::kW;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) rec[w0 + 3 * d + i] = w[i][d];
+  return true;
+}
+
 template <int DIM, typename T, typename Sink>
+__global__ void __launch_bounds__(kThreads) k_p2g_cells(KParams<T> kp, Geom<DIM> g, PView<T> P,
+                                                        const uint32_t* __restrict__ perm,
+                                                        const int4* __restrict__ chunks,
+                                                        const WsHeader* __restrict__ hdr, Sink sink, int32_t* status,
+                                                        uint32_t* fallbacks) {
+  constexpr int RF = RecLayout<DIM>::kFloats;
+  constexpr int RS = RecLayout<DIM>::kStride;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int TN = tile_nodes<DIM>(g);
+  T* tile = reinterpret_cast<T*>(smem_raw);
+  T* recs = tile + 4 * TN;                                          // [kChunk][RS]
+  int* cells = reinterpret_cast<int*>(recs + (size_t)kChunk * RS);  // [kChunk]
+  int* runs = cells + kChunk;                                       // [kChunk + 1]
+  __shared__ int nruns_s;
+  __shared__ int warp_cnt[kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t nch = hdr->n_chunks;
+  const uint32_t per = (nch + gridDim.x - 1) / gridDim.x;
+  const uint32_t c0 = blockIdx.x * per;
+  const uint32_t c1 = min(nch, c0 + per);
+  const TileAdder<DIM, T> tacc{tile, TN, g.tile};
+  int cur = -1;
+  int org[DIM];
+  for (uint32_t c = c0; c < c1; ++c) {
+    const int4 ch = chunks[c];
+    if (ch.x != cur) {
+      if (cur >= 0) {
+        __syncthreads();
+        p2g_flush<DIM, T, Sink>(tile, TN, g, org, sink);
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < 4 * TN; t += blockDim.x) tile[t] = T(0);
+      cur = ch.x;
+      int bc[DIM];
+      block_coords<DIM>(g, cur, bc);
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) org[d] = bc[d] * g.bs;
+    }
+    // phase 1: one record per particle (cell -1 marks a particle that failed the bounds check)
+    for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {
+      T rec[RS];
+      int cell = -1;
+      if (!p2g_record<DIM, T>(kp, g, P, perm[ch.y + l], org, rec, cell, status, fallbacks)) cell = -1;
+#pragma unroll
+      for (int i = 0; i < RF; ++i) recs[(size_t)l * RS + i] = rec[i];
+      cells[l] = cell;
+    }
+    __syncthreads();
+    // phase 2: run heads (a particle whose cell differs from its predecessor's), compacted in
+    // order; runs[nruns] = chunk size, so run r spans [runs[r], runs[r + 1]).  Particles that failed
+    // the bounds check (cell -1) form runs of their own, skipped below.
+    {
+      const int per_t = (ch.z + blockDim.x - 1) / blockDim.x;  // <= 2 for kChunk = 512
+      const int beg = threadIdx.x * per_t;
+      int heads = 0;
+      for (int l = beg; l < min(ch.z, beg + per_t); ++l) heads += (l == 0 || cells[l] != cells[l - 1]);
+      int inc = heads;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+      }
+      if (lane == 31) warp_cnt[warp] = inc;
+      __syncthreads();
+      int before = 0, tot = 0;
+#pragma unroll
+      for (int w = 0; w < kThreads / 32; ++w) {
+        before += w < warp ? warp_cnt[w] : 0;
+        tot += warp_cnt[w];
+      }
+      int r = before + inc - heads;
+      for (int l = beg; l < min(ch.z, beg + per_t); ++l)
+        if (l == 0 || cells[l] != cells[l - 1]) runs[r++] = l;
+      if (threadIdx.x == 0) {
+        nruns_s = tot;
+        runs[tot] = ch.z;
+      }
+    }
+    __syncthreads();
+    const int nruns = nruns_s;
+    // phase 3: a warp per run, a lane per stencil node (2D: three particles at a time, 9 lanes each)
+    constexpr int NODES = DIM == 3 ? 27 : 9;
+    const int grp = lane / NODES;          // 3D: 0 (lanes 0..26); 2D: 0..2 (lanes 0..26)
+    const int o = lane - grp * NODES;
+    const bool node_lane = lane < 27;
+    const int oi = DIM == 3 ? o / 9 : o / 3, oj = DIM == 3 ? (o / 3) % 3 : o % 3, ok = DIM == 3 ? o % 3 : 0;
+    constexpr int GSTEP = DIM == 3 ? 1 : 3;
+    constexpr int a0 = DIM == 3 ? 4 : 3;
+    constexpr int w0 = RecLayout<DIM>::kW;
+    for (int r = warp; r < nruns; r += kThreads / 32) {
+      const int l0 = runs[r], l1 = runs[r + 1];
+      if (cells[l0] < 0) continue;
+      T am = T(0), a_0 = T(0), a_1 = T(0), a_2 = T(0);
+      if (node_lane) {
+        for (int l = l0 + grp; l < l1; l += GSTEP) {
+          const T* rc = recs + (size_t)l * RS;
+          T wgt;
+          if constexpr (DIM == 3)
+            wgt = rc[w0 + oi] * rc[w0 + 3 + oj] * rc[w0 + 6 + ok];
+          else
+            wgt = rc[w0 + oi] * rc[w0 + 3 + oj];
+          const T m = rc[0];
+          if constexpr (DIM == 3) {
+            const T t0 = rc[1] + rc[a0 + 0] * T(oi) + rc[a0 + 1] * T(oj) + rc[a0 + 2] * T(ok);
+            const T t1 = rc[2] + rc[a0 + 3] * T(oi) + rc[a0 + 4] * T(oj) + rc[a0 + 5] * T(ok);
+            const T t2 = rc[3] + rc[a0 + 6] * T(oi) + rc[a0 + 7] * T(oj) + rc[a0 + 8] * T(ok);
+            a_0 += wgt * t0;
+            a_1 += wgt * t1;
+            a_2 += wgt * t2;
+          } else {
+            const T t0 = rc[1] + rc[a0 + 0] * T(oi) + rc[a0 + 1] * T(oj);
+            const T t1 = rc[2] + rc[a0 + 2] * T(oi) + rc[a0 + 3] * T(oj);
+            a_0 += wgt * t0;
+            a_1 += wgt * t1;
+          }
+          am += wgt * m;
+        }
+      }
+      if constexpr (DIM == 2) {
+        // fold the three particle groups onto lanes 0..8
+#pragma unroll
+        for (int gsrc = 1; gsrc < 3; ++gsrc) {
+          const T b0 = __shfl_down_sync(0xffffffffu, a_0, 9 * gsrc), b1 = __shfl_down_sync(0xffffffffu, a_1, 9 * gsrc);
+          const T bm = __shfl_down_sync(0xffffffffu, am, 9 * gsrc);
+          if (lane < 9) {
+            a_0 += b0;
+            a_1 += b1;
+            am += bm;
+          }
+        }
+      }
+      if (lane < NODES) {
+        const int cl = cells[l0];
+        int lb[DIM];
+        if constexpr (DIM == 3) {
+          lb[2] = cl % g.bs;
+          lb[1] = (cl / g.bs) % g.bs;
+          lb[0] = cl / (g.bs * g.bs);
+          tacc.add(lb[0] + oi, lb[1] + oj, lb[2] + ok, a_0, a_1, a_2, am);
+        } else {
+          lb[1] = cl % g.bs;
+          lb[0] = cl / g.bs;
+          tacc.add(lb[0] + oi, lb[1] + oj, 0, a_0, a_1, T(0), am);
+        }
+      }
+    }
+    __syncthreads();  // records and runs are rewritten by the next chunk
+  }
+  if (cur >= 0) {
+    __syncthreads();
+    p2g_flush<DIM, T, Sink>(tile, TN, g, org, sink);
+  }
+}
+
+template <int DIM, typename T, typename Sink, bool kDirect>
 __global__ void __launch_bounds__(kThreads) k_p2g(KParams<T> kp, Geom<DIM> g, PView<T> P,
                                                   const uint32_t* __restrict__ perm, const int4* __restrict__ chunks,
                                                   const WsHeader* __restrict__ hdr, Sink sink, int32_t* status,
@@ -388,6 +645,22 @@ __global__ void __launch_bounds__(kThreads) k_p2g(KParams<T> kp, Geom<DIM> g, PV
   const uint32_t per = (nch + gridDim.x - 1) / gridDim.x;
   const uint32_t c0 = blockIdx.x * per;
   const uint32_t c1 = min(nch, c0 + per);
+  if constexpr (kDirect) {
+    for (uint32_t c = c0; c < c1; ++c) {
+      const int4 ch = chunks[c];
+      DirectAdder<DIM, T, Sink> acc;
+      acc.sink = sink;
+      acc.R = g.R;
+      int bc[DIM];
+      block_coords<DIM>(g, ch.x, bc);
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) acc.org[d] = bc[d] * g.bs;
+      for (int l = threadIdx.x; l < ch.z; l += blockDim.x)
+        p2g_particle<DIM, T>(kp, g, P, perm[ch.y + l], acc.org, acc, status, fallbacks);
+    }
+    return;
+  }
+  const TileAdder<DIM, T> tacc{tile, TN, g.tile};
   int cur = -1;
   int org[DIM];
   for (uint32_t c = c0; c < c1; ++c) {
@@ -407,7 +680,7 @@ __global__ void __launch_bounds__(kThreads) k_p2g(KParams<T> kp, Geom<DIM> g, PV
       __syncthreads();
     }
     for (int l = threadIdx.x; l < ch.z; l += blockDim.x)
-      p2g_particle<DIM, T>(kp, g, P, perm[ch.y + l], org, tile, TN, status, fallbacks);
+      p2g_particle<DIM, T>(kp, g, P, perm[ch.y + l], org, tacc, status, fallbacks);
   }
   if (cur >= 0) {
     __syncthreads();
@@ -526,18 +799,36 @@ struct G2PExtra {
   int cell_bits;
 };
 
+// The state G2P reads of one particle (loaded ahead of the arithmetic so that the loads of
+// several particles are in flight together).
+template <int DIM, typename T>
+struct G2PIn {
+  T x[DIM];
+  T F[DIM * DIM];
+  T jp;
+};
+
+template <int DIM, typename T>
+__device__ __forceinline__ void g2p_load(const PView<T>& Pin, uint32_t p, bool need_jp, G2PIn<DIM, T>& in) {
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) in.x[d] = Pin.x[(size_t)p * DIM + d];
+#pragma unroll
+  for (int i = 0; i < DIM * DIM; ++i) in.F[i] = Pin.F[(size_t)p * DIM * DIM + i];
+  in.jp = need_jp ? Pin.Jp[p] : T(1);
+}
+
 template <int DIM, typename T>
 __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DIM>& g, const PView<T>& Pin,
                                              const PView<T>& Pout, uint32_t p, uint32_t q, const int org[DIM],
                                              const Node4<T>* tile, int32_t* status, bool sorted,
-                                             const G2PExtra& ex) {
+                                             const G2PExtra& ex, const G2PIn<DIM, T>& in) {
   constexpr int DD = DIM * DIM;
   T xp[DIM], fx[DIM], w[3][DIM];
   int lb[DIM];
   bool ok = true;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
-    xp[d] = Pin.x[(size_t)p * DIM + d];
+    xp[d] = in.x[d];
     int b;
     ok = ok && base_of(xp[d], kp.inv_dx, kp.res, b, fx[d]);
     lb[d] = b - org[d];
@@ -603,7 +894,7 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
   for (int i = 0; i < DD; ++i) Cn[i] *= c4;
   T F[DD], Fn[DD];
 #pragma unroll
-  for (int i = 0; i < DD; ++i) F[i] = Pin.F[(size_t)p * DD + i];
+  for (int i = 0; i < DD; ++i) F[i] = in.F[i];
   // F <- (I + dt C) F   (g2p.py:46)
 #pragma unroll
   for (int r = 0; r < DIM; ++r)
@@ -614,9 +905,8 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
       for (int k = 0; k < DIM; ++k) acc += ((r == k ? T(1) : T(0)) + kp.dt * Cn[r * DIM + k]) * F[k * DIM + c];
       Fn[r * DIM + c] = acc;
     }
-  T jp_new = T(1);
   const bool write_jp = (DIM == 2) || sorted || kp.model == FFMPM_MODEL_SNOW;
-  if (write_jp) jp_new = Pin.Jp[p];
+  T jp_new = in.jp;
   if constexpr (DIM == 2) {
     // two_d/g2p.py:37-46: SVD, clamp (snow only), rebuild, Jp update.  Without the clamp the
     // rebuild returns F itself (up to the sign convention of the SVD), so only snow rebuilds.
@@ -744,11 +1034,19 @@ __global__ void __launch_bounds__(kThreads) k_g2p(KParams<T> kp, Geom<DIM> g, PV
         __syncthreads();
       }
     }
-    for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {
-      const uint32_t s = ch.y + l;
-      const uint32_t p = perm[s];
-      const uint32_t q = kSorted ? s : p;
-      g2p_particle<DIM, T>(kp, g, Pin, Pout, p, q, org, tile, status, kSorted, ex);
+    const bool need_jp = (DIM == 2) || kSorted || kp.model == FFMPM_MODEL_SNOW;
+    // two particles per thread per iteration: both particles' loads are issued before either
+    // one's arithmetic
+    for (int l = threadIdx.x; l < ch.z; l += 2 * blockDim.x) {
+      const int l2 = l + blockDim.x;
+      const bool two = l2 < ch.z;
+      const uint32_t s1 = ch.y + l, s2 = ch.y + (two ? l2 : l);
+      const uint32_t p1 = perm[s1], p2 = perm[s2];
+      G2PIn<DIM, T> in1, in2;
+      g2p_load<DIM, T>(Pin, p1, need_jp, in1);
+      g2p_load<DIM, T>(Pin, p2, need_jp, in2);
+      g2p_particle<DIM, T>(kp, g, Pin, Pout, p1, kSorted ? s1 : p1, org, tile, status, kSorted, ex, in1);
+      if (two) g2p_particle<DIM, T>(kp, g, Pin, Pout, p2, kSorted ? s2 : p2, org, tile, status, kSorted, ex, in2);
     }
   }
 }

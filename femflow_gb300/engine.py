@@ -37,12 +37,12 @@ def real_bytes(dtype) -> int:
 def make_params(dim: int, res: int, dtype, dx: float, inv_dx: float, dt: float, gravity: float = 0.0,
                 volume: float = 1.0, hardening: float = 1.0, mass: float = 0.0, mu_0: float = 0.0,
                 lambda_0: float = 0.0, model="neo_hookean", wall_mode="reference", deterministic: bool = False,
-                block_size: int = 0) -> N.Params:
+                block_size: int = 0, variant: int = 0) -> N.Params:
     p = N.Params()
     p.dim, p.res, p.real_bytes = int(dim), int(res), real_bytes(dtype)
     p.model = N.MODELS[model] if isinstance(model, str) else int(model)
     p.wall_mode = N.WALLS[wall_mode] if isinstance(wall_mode, str) else int(wall_mode)
-    p.deterministic, p.block_size = int(bool(deterministic)), int(block_size)
+    p.deterministic, p.block_size, p.variant = int(bool(deterministic)), int(block_size), int(variant)
     p.dx, p.inv_dx, p.dt, p.gravity = float(dx), float(inv_dx), float(dt), float(gravity)
     p.volume, p.hardening = float(volume), float(hardening)
     p.mass, p.mu_0, p.lambda_0 = float(mass), float(mu_0), float(lambda_0)

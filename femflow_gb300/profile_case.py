@@ -24,11 +24,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--dtype", choices=["f32", "f64"], default="f32")
+    ap.add_argument("--variant", type=int, default=0, help="kernel variant flags (see ffmpm_params.variant)")
+    ap.add_argument("--block-size", type=int, default=0)
     args = ap.parse_args()
     s = two_cubes(args.n_per_cube)
     dtype = torch.float32 if args.dtype == "f32" else torch.float64
     solver = MPMSolver(torch.tensor(s["x"]), res=args.res, dt=args.dt, gravity=-9.8, volume=s["vol"],
-                       mass=s["mass"], mu_0=s["mu"], lambda_0=s["lam"], v=torch.tensor(s["v"]), dtype=dtype)
+                       mass=s["mass"], mu_0=s["mu"], lambda_0=s["lam"], v=torch.tensor(s["v"]), dtype=dtype,
+                       variant=args.variant, block_size=args.block_size)
     solver.step(args.warmup)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -36,8 +39,11 @@ def main():
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     solver.check()
+    prof = solver.profile(args.steps)
+    per = {k: round(v[0] / v[1] * 1e3, 2) for k, v in prof.items() if v[1]}
     print(f"profile_case: {s['n']} particles, res {args.res}, {args.steps} substeps in {dt * 1e3:.2f} ms "
-          f"({s['n'] * args.steps / dt:.3e} particle-substeps/s), plan {solver.plan_info()}")
+          f"({s['n'] * args.steps / dt:.3e} particle-substeps/s), plan {solver.plan_info()}, "
+          f"us per launch {per}")
 
 
 if __name__ == "__main__":

@@ -44,7 +44,7 @@ class MPMSolver:
     def __init__(self, x, *, res: int, dt: float, gravity: float = -9.8, volume: float = 1.0,
                  hardening: float = 1.0, mass=1.0, mu_0=0.0, lambda_0=0.0, v=None, F=None, C=None, Jp=None,
                  dtype=torch.float32, device="cuda", model="neo_hookean", wall_mode="reference",
-                 block_size: int = 0):
+                 block_size: int = 0, variant: int = 0, deterministic: bool = False):
         E._require_cuda()
         device = torch.device(device)
         x = torch.as_tensor(x)
@@ -55,7 +55,7 @@ class MPMSolver:
         self.params = E.make_params(dim, res, dtype, dx, float(res), dt, gravity, volume, hardening,
                                     0.0 if per_particle else float(mass), 0.0 if per_particle else float(mu_0),
                                     0.0 if per_particle else float(lambda_0), model=model, wall_mode=wall_mode,
-                                    block_size=block_size)
+                                    block_size=block_size, variant=variant, deterministic=deterministic)
         self._a = _Buffers(n, dim, dtype, device, per_particle)
         self._b = _Buffers(n, dim, dtype, device, per_particle)
         a = self._a

@@ -60,7 +60,7 @@ typedef struct ffmpm_params {
   int32_t wall_mode;    /* FFMPM_WALLS_* */
   int32_t deterministic;/* 1: P2G sums in a fixed order (bit-identical across runs) */
   int32_t block_size;   /* nodes per block side for work assignment; 0 = default */
-  int32_t reserved;
+  int32_t variant;      /* kernel variant flags chosen by the autotuner; 0 = default */
   double dx, inv_dx, dt;
   double gravity;       /* added to the axis-1 (y) grid velocity, as the reference */
   double volume;        /* particle volume (reference argument `volume`) */

@@ -30,8 +30,8 @@ def host_keys(x32, res, bs, det):
     for dd in range(x32.shape[1]):
         blk = blk * nb + b[:, dd] // bs
         cell = cell * bs + b[:, dd] % bs
-    cbits = x32.shape[1] * int(np.log2(bs)) if det else 0
-    key = (blk << cbits) | cell if det else blk
+    cbits = x32.shape[1] * int(np.log2(bs))  # keys order by block, then by cell inside the block
+    key = (blk << cbits) | cell
     key = np.where(valid, key, 0xFFFFFFFF).astype(np.uint64)
     return key
 
@@ -66,13 +66,14 @@ def _scene(dtype, n_per=3000, res=32):
     return s
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2])
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
-def test_sorted_solver_matches_in_place_substeps(dtype):
+def test_sorted_solver_matches_in_place_substeps(dtype, variant):
     s = _scene(dtype)
     res, dt, g, steps = s["res"], 2e-4, -9.8, 10
     solver = MPMSolver(torch.tensor(s["x"]), res=res, dt=dt, gravity=g, volume=s["vol"],
                        mass=torch.tensor(s["mass"]), mu_0=torch.tensor(s["mu"]), lambda_0=torch.tensor(s["lam"]),
-                       v=torch.tensor(s["v"]), dtype=dtype)
+                       v=torch.tensor(s["v"]), dtype=dtype, variant=variant)
     solver.step(steps, check=True)
     got = solver.state()
     N_ = len(s["x"])
