@@ -117,12 +117,17 @@ def measured_peak_hbm():
 
 def ncu_traffic():
     """Per-launch DRAM bytes of the profiled kernels, from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "traffic_two_cubes.json")
+    path = os.path.join(ROOT, "profiles", "traffic_two_cubes.txt")
+    out = {}
     try:
         with open(path) as f:
-            return json.load(f)
+            for line in f:
+                parts = line.split()
+                if len(parts) == 2 and not line.startswith("#"):
+                    out[parts[0]] = int(parts[1])
     except (OSError, ValueError):
-        return {}
+        pass
+    return out
 
 
 # --------------------------------------------------------------------------- ours
@@ -206,7 +211,7 @@ def run_ours(args):
     ps = ParticleSet(st["x"], torch.full((n,), s["mass"], device=dev), torch.full((n,), s["mu"], device=dev),
                      torch.full((n,), s["lam"], device=dev))
     three_d.p2g(float(RES), 1.0, 1 / RES, DT, s["vol"], gv, gm, ps, st["v"], st["F"], st["C"],
-                st["Jp"].view(n, 1))
+                st["Jp"].view(n, 1).contiguous())
     active = int((gm > 0).sum().item())
     del gv, gm
     alg = {"p2g": n * 96 + active * 16, "g2p": n * 144 + active * 12}

@@ -49,7 +49,7 @@ class Params(ctypes.Structure):
 class Particles(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("x", ctypes.c_void_p), ("v", ctypes.c_void_p), ("F", ctypes.c_void_p),
                 ("C", ctypes.c_void_p), ("Jp", ctypes.c_void_p), ("mass", ctypes.c_void_p), ("mu_0", ctypes.c_void_p),
-                ("lambda_0", ctypes.c_void_p)]
+                ("lambda_0", ctypes.c_void_p), ("stride", ctypes.c_int64)]
 
 
 class Grid(ctypes.Structure):

@@ -168,6 +168,7 @@ PView<T> pview(const ffmpm_particles& P) {
   v.mass = static_cast<T*>(const_cast<void*>(P.mass));
   v.mu0 = static_cast<T*>(const_cast<void*>(P.mu_0));
   v.lam0 = static_cast<T*>(const_cast<void*>(P.lambda_0));
+  v.soa = P.stride;
   return v;
 }
 
@@ -273,7 +274,7 @@ struct PhaseTimer {
 
 // keys -> sort -> plan.  Leaves the permutation pointer in *perm.
 template <int DIM, typename T>
-void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const T* x, bool keys_ready,
+void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<T>& x, bool keys_ready,
                    const uint32_t** perm, cudaStream_t s, PhaseTimer* tm = nullptr) {
   const KParams<T> kp = kparams<T>(p);
   const Geom<DIM> g = geom<DIM>(L);
@@ -359,7 +360,7 @@ template <int DIM, typename T>
 int op_substep(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_particles* P, cudaStream_t s) {
   const PView<T> pv = pview<T>(*P);
   const uint32_t* perm = nullptr;
-  sort_and_plan<DIM, T>(p, L, w, pv.x, false, &perm, s);
+  sort_and_plan<DIM, T>(p, L, w, pv, false, &perm, s);
   launch_p2g<DIM, T>(p, L, w, pv, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s);
   launch_grid_update<DIM, T>(p, L, w, s);
   G2PExtra ex{};
@@ -377,7 +378,7 @@ int op_substeps_sorted(const ffmpm_params& p, const Layout& L, const Ws& w, ffmp
     const int32_t* ids_in = (k & 1) ? ids_b : ids_a;
     int32_t* ids_out = (k & 1) ? ids_a : ids_b;
     const uint32_t* perm = nullptr;
-    sort_and_plan<DIM, T>(p, L, w, in.x, k > 0, &perm, s, tm);
+    sort_and_plan<DIM, T>(p, L, w, in, k > 0, &perm, s, tm);
     if (tm) tm->begin(3);
     launch_p2g<DIM, T>(p, L, w, in, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s);
     if (tm) tm->end(1);
@@ -401,7 +402,7 @@ int op_p2g(const ffmpm_params& p, const Layout& L, const Ws& w, const ffmpm_part
            cudaStream_t s) {
   const PView<T> pv = pview<T>(*P);
   const uint32_t* perm = nullptr;
-  sort_and_plan<DIM, T>(p, L, w, pv.x, false, &perm, s);
+  sort_and_plan<DIM, T>(p, L, w, pv, false, &perm, s);
   launch_p2g<DIM, T>(p, L, w, pv, perm, UserSink<T, DIM>{static_cast<T*>(grid->velocity), static_cast<T*>(grid->mass)},
                      s);
   return check_launch();
@@ -412,7 +413,7 @@ int op_g2p(const ffmpm_params& p, const Layout& L, const Ws& w, const ffmpm_grid
            cudaStream_t s) {
   const PView<T> pv = pview<T>(*P);
   const uint32_t* perm = nullptr;
-  sort_and_plan<DIM, T>(p, L, w, pv.x, false, &perm, s);
+  sort_and_plan<DIM, T>(p, L, w, pv, false, &perm, s);
   G2PExtra ex{};
   int rc = launch_g2p<DIM, T, false, false>(p, L, w, pv, pv, perm, static_cast<const T*>(grid->velocity), ex, s);
   return rc != FFMPM_OK ? rc : check_launch();
@@ -434,8 +435,10 @@ int op_sort(const ffmpm_params& p, const Layout& L, const Ws& w, const void* x, 
   const KParams<T> kp = kparams<T>(p);
   const Geom<DIM> g = geom<DIM>(L);
   const uint32_t n = (uint32_t)L.n;
-  k_keys<DIM, T><<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kp, g, static_cast<const T*>(x), n, L.cell_bits,
-                                                                     w.keys_next, nullptr, &w.hdr->status);
+  PView<T> xv{};
+  xv.x = static_cast<T*>(const_cast<void*>(x));
+  k_keys<DIM, T><<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kp, g, xv, n, L.cell_bits, w.keys_next, nullptr,
+                                                                     &w.hdr->status);
   const uint32_t *ks = nullptr, *perm = nullptr;
   radix_sort(w.keys_next, n, L.passes, L.digit_bits, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, s, &ks, &perm);
   if (keys_out) cudaMemcpyAsync(keys_out, ks, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
@@ -483,6 +486,7 @@ FFMPM_OP(DiagOp, op_diag)
 
 bool particles_ok(const ffmpm_params& p, const ffmpm_particles* P, bool need_jp) {
   if (!P || P->n < 0) return false;
+  if (P->stride != 0 && P->stride < P->n) return false;
   if (P->n == 0) return true;
   if (!P->x || !P->v || !P->F || !P->C) return false;
   if (need_jp && !P->Jp) return false;

@@ -120,8 +120,18 @@ __device__ __forceinline__ void cofactor3(const T m[9], T c[9]) {
 // factor of any nonsingular F, including det F < 0, where R is a reflection exactly as
 // U @ Vh from an SVD (linear_algebra.py:131-132).  Returns the number of iterations, or -1 when F
 // is (numerically) singular or the iteration did not settle.
+__device__ __forceinline__ float ffrcp(float a) { return __frcp_rn(a); }
+__device__ __forceinline__ double ffrcp(double a) { return __drcp_rn(a); }
+
+__device__ __forceinline__ float ffrsqrt_approx(float a) { return rsqrtf(a); }
+__device__ __forceinline__ double ffrsqrt_approx(double a) { return rsqrt(a); }
+
+// Newton iteration for the orthogonal polar factor (see polar3).  `degenerate_ratio`: when > 0,
+// the call returns -2 without iterating if |det F| <= degenerate_ratio * (|F|_F / sqrt 3)^3
+// (F close to singular relative to its size).  Returns the number of iterations, or -1 when the
+// iteration did not settle / F is singular.
 template <typename T>
-__device__ __forceinline__ int polar3_newton(const T F[9], T R[9], int max_iter) {
+__device__ __forceinline__ int polar3_newton(const T F[9], T R[9], int max_iter, T degenerate_ratio = T(0)) {
   T X[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) X[i] = F[i];
@@ -130,16 +140,29 @@ __device__ __forceinline__ int polar3_newton(const T F[9], T R[9], int max_iter)
     T cof[9];
     cofactor3(X, cof);
     const T det = X[0] * cof[0] + X[1] * cof[1] + X[2] * cof[2];
-    T nx = 0, nc = 0;
+    // Frobenius scaling g = (|X^{-1}|_F / |X|_F)^(1/2) speeds up the first iterations; close to the
+    // solution g -> 1, so later iterations are unscaled.  Any positive g leaves the fixed point
+    // unchanged, so g is computed with approximate square roots.
+    T g = T(1);
+    if (it < 2) {
+      T nx = 0, nc = 0;
 #pragma unroll
-    for (int i = 0; i < 9; ++i) {
-      nx += X[i] * X[i];
-      nc += cof[i] * cof[i];
+      for (int i = 0; i < 9; ++i) {
+        nx += X[i] * X[i];
+        nc += cof[i] * cof[i];
+      }
+      if (it == 0 && degenerate_ratio > T(0)) {
+        // (|F|/sqrt3)^3 = nx^(3/2) / 5.196
+        if (!(ffabs(det) > degenerate_ratio * nx * ffsqrt(nx) * T(0.19245009))) return -2;
+      }
+      if (!(nx > T(0)) || !(ffabs(det) > T(0))) return -1;
+      // g^4 = |cof|^2 / (det^2 |X|^2)
+      const T g4 = nc * ffrcp(det * det * nx);
+      g = ffrcp(ffrsqrt_approx(ffrsqrt_approx(g4)));  // g4^(1/4)
+    } else if (!(ffabs(det) > T(0))) {
+      return -1;
     }
-    if (!(ffabs(det) > T(0)) || !(nx > T(0))) return -1;
-    const T inv_det = T(1) / det;
-    // ||X^{-T}||_F = ||cof||_F / |det|;  g = sqrt(||X^{-1}|| / ||X||)
-    T g = ffsqrt(ffsqrt(nc * inv_det * inv_det / nx));
+    const T inv_det = ffrcp(det);
     const T ha = T(0.5) * g, hb = T(0.5) * inv_det / g;
     T diff = 0;
 #pragma unroll
@@ -161,19 +184,12 @@ __device__ __forceinline__ int polar3_newton(const T F[9], T R[9], int max_iter)
 }
 
 // Polar factor used by the stress.  In float, F whose smallest singular value is small relative
-// to its largest (|det F| / (|F|_F/sqrt 3)^3 below 1e-3) or where the float iteration fails is
-// redone in double; `fallbacks` counts those particles.
+// to its largest (|det F| / (|F|_F/sqrt 3)^3 at most 1e-3) or where the float iteration does not
+// settle is redone in double; `fallbacks` counts those particles.
 template <typename T>
 __device__ __forceinline__ void polar3(const T F[9], T R[9], uint32_t* fallbacks) {
   if constexpr (sizeof(T) == 4) {
-    T n2 = 0;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) n2 += F[i] * F[i];
-    const T d = det3(F);
-    const T s3 = n2 * ffsqrt(n2) * T(0.19245009);  // (|F|_F / sqrt 3)^3 = |F|_F^3 / 5.196
-    bool need64 = !(ffabs(d) > T(1e-3) * s3);
-    if (!need64) need64 = polar3_newton(F, R, 12) < 0;
-    if (need64) {
+    if (polar3_newton(F, R, 12, T(1e-3)) < 0) {
       double Fd[9], Rd[9];
 #pragma unroll
       for (int i = 0; i < 9; ++i) Fd[i] = double(F[i]);

@@ -34,6 +34,11 @@ template <typename T>
 struct PView {
   T *x, *v, *F, *C, *Jp;
   T *mass, *mu0, *lam0;  // nullable: scalar material from KParams
+  int64_t soa;           // 0: row-major [n][k] (the reference's layout); > 0: component-major stride
+  // index of component c (of k) of particle p
+  __device__ __forceinline__ size_t at(uint32_t p, int c, int k) const {
+    return soa ? (size_t)c * (size_t)soa + p : (size_t)p * k + c;
+  }
 };
 
 template <int DIM>
@@ -84,7 +89,7 @@ __device__ __forceinline__ bool particle_key(const T* xp, const KParams<T>& kp, 
 }
 
 template <int DIM, typename T>
-__global__ void __launch_bounds__(kThreads) k_keys(KParams<T> kp, Geom<DIM> g, const T* __restrict__ x, uint32_t n,
+__global__ void __launch_bounds__(kThreads) k_keys(KParams<T> kp, Geom<DIM> g, PView<T> P, uint32_t n,
                                                    int cell_bits, uint32_t* __restrict__ keys,
                                                    uint32_t* __restrict__ block_count, int32_t* status) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -93,7 +98,7 @@ __global__ void __launch_bounds__(kThreads) k_keys(KParams<T> kp, Geom<DIM> g, c
   if (i < n) {
     T xp[DIM];
 #pragma unroll
-    for (int d = 0; d < DIM; ++d) xp[d] = x[(size_t)i * DIM + d];
+    for (int d = 0; d < DIM; ++d) xp[d] = P.x[P.at(i, d, DIM)];
     valid = particle_key<DIM, T>(xp, kp, g, cell_bits, key, blk);
     if (!valid) raise_status(status, FFMPM_STATUS_OOB);
     keys[i] = key;
@@ -319,7 +324,7 @@ __device__ __forceinline__ void p2g_particle(const KParams<T>& kp, const Geom<DI
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     int b;
-    ok = ok && base_of(P.x[(size_t)p * DIM + d], kp.inv_dx, kp.res, b, fx[d]);
+    ok = ok && base_of(P.x[P.at(p, d, DIM)], kp.inv_dx, kp.res, b, fx[d]);
     lb[d] = b - org[d];
     ok = ok && lb[d] >= 0 && lb[d] + 2 < g.tile;
     T ww[3];
@@ -337,11 +342,11 @@ __device__ __forceinline__ void p2g_particle(const KParams<T>& kp, const Geom<DI
   T F[DD], C[DD], A[DD], v[DIM];
 #pragma unroll
   for (int i = 0; i < DD; ++i) {
-    F[i] = P.F[(size_t)p * DD + i];
-    C[i] = P.C[(size_t)p * DD + i];
+    F[i] = P.F[P.at(p, i, DD)];
+    C[i] = P.C[P.at(p, i, DD)];
   }
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) v[d] = P.v[(size_t)p * DIM + d];
+  for (int d = 0; d < DIM; ++d) v[d] = P.v[P.at(p, d, DIM)];
   affine_of<DIM, T>(kp, F, C, m, mu, lam, A, fallbacks);
   const T dx = kp.dx;
   T mv[DIM];
@@ -417,9 +422,11 @@ __device__ __forceinline__ void p2g_flush(const T* tile, int TN, const Geom<DIM>
 template <int DIM>
 struct RecLayout {
   static constexpr int kFloats = DIM == 3 ? 22 : 13;  // m, q (DIM), dx A (DIM^2), weights (3 DIM)
-  static constexpr int kStride = DIM == 3 ? 25 : 13;  // odd: the per-thread stores hit distinct banks
+  // 7 (3D) / 5 (2D) float4 per record: 16-byte aligned vector accesses, and the per-thread vector
+  // stores of phase 1 fall on distinct bank groups (stride 112 B / 80 B).
+  static constexpr int kStride = DIM == 3 ? 28 : 20;
+  static constexpr int kW = DIM == 3 ? 13 : 7;  // first weight
   static_assert(kFloats == 1 + DIM + DIM * DIM + 3 * DIM, "record size");
-  static constexpr int kW = DIM == 3 ? 13 : 7;        // first weight
 };
 
 template <int DIM, typename T>
@@ -433,7 +440,7 @@ __device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     int b;
-    ok = ok && base_of(P.x[(size_t)p * DIM + d], kp.inv_dx, kp.res, b, fx[d]);
+    ok = ok && base_of(P.x[P.at(p, d, DIM)], kp.inv_dx, kp.res, b, fx[d]);
     lb[d] = b - org[d];
     ok = ok && lb[d] >= 0 && lb[d] + 2 < g.tile;
     T ww[3];
@@ -452,11 +459,11 @@ __device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>
   T F[DD], C[DD], A[DD], v[DIM];
 #pragma unroll
   for (int i = 0; i < DD; ++i) {
-    F[i] = P.F[(size_t)p * DD + i];
-    C[i] = P.C[(size_t)p * DD + i];
+    F[i] = P.F[P.at(p, i, DD)];
+    C[i] = P.C[P.at(p, i, DD)];
   }
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) v[d] = P.v[(size_t)p * DIM + d];
+  for (int d = 0; d < DIM; ++d) v[d] = P.v[P.at(p, d, DIM)];
   affine_of<DIM, T>(kp, F, C, m, mu, lam, A, fallbacks);
   const T dx = kp.dx;
   rec[0] = m;
@@ -523,7 +530,10 @@ __global__ void __launch_bounds__(kThreads) k_p2g_cells(KParams<T> kp, Geom<DIM>
       int cell = -1;
       if (!p2g_record<DIM, T>(kp, g, P, perm[ch.y + l], org, rec, cell, status, fallbacks)) cell = -1;
 #pragma unroll
-      for (int i = 0; i < RF; ++i) recs[(size_t)l * RS + i] = rec[i];
+      for (int i = RF; i < RS; ++i) rec[i] = T(0);
+      Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)l * RS);
+#pragma unroll
+      for (int i = 0; i < RS / 4; ++i) dst[i] = Node4<T>{rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]};
       cells[l] = cell;
     }
     __syncthreads();
@@ -559,69 +569,89 @@ __global__ void __launch_bounds__(kThreads) k_p2g_cells(KParams<T> kp, Geom<DIM>
     }
     __syncthreads();
     const int nruns = nruns_s;
-    // phase 3: a warp per run, a lane per stencil node (2D: three particles at a time, 9 lanes each)
-    constexpr int NODES = DIM == 3 ? 27 : 9;
-    const int grp = lane / NODES;          // 3D: 0 (lanes 0..26); 2D: 0..2 (lanes 0..26)
-    const int o = lane - grp * NODES;
-    const bool node_lane = lane < 27;
-    const int oi = DIM == 3 ? o / 9 : o / 3, oj = DIM == 3 ? (o / 3) % 3 : o % 3, ok = DIM == 3 ? o % 3 : 0;
-    constexpr int GSTEP = DIM == 3 ? 1 : 3;
-    constexpr int a0 = DIM == 3 ? 4 : 3;
+    // phase 3: a warp per run.  A particle is served by LP lanes (3D: 9, one per (j, k); 2D: 3, one
+    // per j); each lane accumulates the 3 nodes along x (i = 0, 1, 2) of its (j, k), and the warp
+    // takes NG particles of the run per step.  The NG partial sums are then folded onto group 0.
+    constexpr int LP = DIM == 3 ? 9 : 3;
+    constexpr int NG = 32 / LP;  // 3 (3D) or 10 (2D) particles per step
+    const int grp = lane / LP;
+    const int jk = lane - grp * LP;
+    const bool active = grp < NG;
+    const int oj = DIM == 3 ? jk / 3 : jk, ok = DIM == 3 ? jk % 3 : 0;
+    constexpr int a0 = 1 + DIM;
     constexpr int w0 = RecLayout<DIM>::kW;
     for (int r = warp; r < nruns; r += kThreads / 32) {
       const int l0 = runs[r], l1 = runs[r + 1];
       if (cells[l0] < 0) continue;
-      T am = T(0), a_0 = T(0), a_1 = T(0), a_2 = T(0);
-      if (node_lane) {
-        for (int l = l0 + grp; l < l1; l += GSTEP) {
-          const T* rc = recs + (size_t)l * RS;
-          T wgt;
-          if constexpr (DIM == 3)
-            wgt = rc[w0 + oi] * rc[w0 + 3 + oj] * rc[w0 + 6 + ok];
-          else
-            wgt = rc[w0 + oi] * rc[w0 + 3 + oj];
-          const T m = rc[0];
-          if constexpr (DIM == 3) {
-            const T t0 = rc[1] + rc[a0 + 0] * T(oi) + rc[a0 + 1] * T(oj) + rc[a0 + 2] * T(ok);
-            const T t1 = rc[2] + rc[a0 + 3] * T(oi) + rc[a0 + 4] * T(oj) + rc[a0 + 5] * T(ok);
-            const T t2 = rc[3] + rc[a0 + 6] * T(oi) + rc[a0 + 7] * T(oj) + rc[a0 + 8] * T(ok);
-            a_0 += wgt * t0;
-            a_1 += wgt * t1;
-            a_2 += wgt * t2;
-          } else {
-            const T t0 = rc[1] + rc[a0 + 0] * T(oi) + rc[a0 + 1] * T(oj);
-            const T t1 = rc[2] + rc[a0 + 2] * T(oi) + rc[a0 + 3] * T(oj);
-            a_0 += wgt * t0;
-            a_1 += wgt * t1;
-          }
-          am += wgt * m;
-        }
-      }
-      if constexpr (DIM == 2) {
-        // fold the three particle groups onto lanes 0..8
+      T acc[3][4];
 #pragma unroll
-        for (int gsrc = 1; gsrc < 3; ++gsrc) {
-          const T b0 = __shfl_down_sync(0xffffffffu, a_0, 9 * gsrc), b1 = __shfl_down_sync(0xffffffffu, a_1, 9 * gsrc);
-          const T bm = __shfl_down_sync(0xffffffffu, am, 9 * gsrc);
-          if (lane < 9) {
-            a_0 += b0;
-            a_1 += b1;
-            am += bm;
+      for (int i = 0; i < 3; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = T(0);
+      if (active) {
+        for (int l = l0 + grp; l < l1; l += NG) {
+          const T* rc = recs + (size_t)l * RS;
+          T rv[RS];
+          const Node4<T>* src = reinterpret_cast<const Node4<T>*>(rc);
+#pragma unroll
+          for (int i = 0; i < RS / 4; ++i) {
+            const Node4<T> q4 = src[i];
+            rv[4 * i] = q4.x;
+            rv[4 * i + 1] = q4.y;
+            rv[4 * i + 2] = q4.z;
+            rv[4 * i + 3] = q4.w;
+          }
+          const T m = rv[0];
+          T wjk;
+          if constexpr (DIM == 3) {
+            const T wy = oj == 0 ? rv[w0 + 3] : (oj == 1 ? rv[w0 + 4] : rv[w0 + 5]);
+            const T wz = ok == 0 ? rv[w0 + 6] : (ok == 1 ? rv[w0 + 7] : rv[w0 + 8]);
+            wjk = wy * wz;
+          } else {
+            wjk = oj == 0 ? rv[w0 + 3] : (oj == 1 ? rv[w0 + 4] : rv[w0 + 5]);
+          }
+          // base_r = q_r + a_r1 j (+ a_r2 k); node i adds i * a_r0
+          T base[DIM], step[DIM];
+#pragma unroll
+          for (int rr = 0; rr < DIM; ++rr) {
+            T b = rv[1 + rr] + rv[a0 + rr * DIM + 1] * T(oj);
+            if constexpr (DIM == 3) b += rv[a0 + rr * DIM + 2] * T(ok);
+            base[rr] = b;
+            step[rr] = rv[a0 + rr * DIM];
+          }
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            const T wgt = rv[w0 + i] * wjk;
+#pragma unroll
+            for (int rr = 0; rr < DIM; ++rr) acc[i][rr] += wgt * (base[rr] + T(i) * step[rr]);
+            acc[i][3] += wgt * m;
           }
         }
       }
-      if (lane < NODES) {
+      // fold the NG groups onto group 0 (lanes 0..LP-1)
+#pragma unroll
+      for (int off = 1; off < NG; off <<= 1) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const T t = __shfl_down_sync(0xffffffffu, acc[i][c], off * LP);
+            if (grp % (2 * off) == 0 && grp + off < NG) acc[i][c] += t;
+          }
+      }
+      if (grp == 0) {
         const int cl = cells[l0];
         int lb[DIM];
         if constexpr (DIM == 3) {
           lb[2] = cl % g.bs;
           lb[1] = (cl / g.bs) % g.bs;
           lb[0] = cl / (g.bs * g.bs);
-          tacc.add(lb[0] + oi, lb[1] + oj, lb[2] + ok, a_0, a_1, a_2, am);
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+            tacc.add(lb[0] + i, lb[1] + oj, lb[2] + ok, acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
         } else {
           lb[1] = cl % g.bs;
           lb[0] = cl / g.bs;
-          tacc.add(lb[0] + oi, lb[1] + oj, 0, a_0, a_1, T(0), am);
+#pragma unroll
+          for (int i = 0; i < 3; ++i) tacc.add(lb[0] + i, lb[1] + oj, 0, acc[i][0], acc[i][1], T(0), acc[i][3]);
         }
       }
     }
@@ -811,9 +841,9 @@ struct G2PIn {
 template <int DIM, typename T>
 __device__ __forceinline__ void g2p_load(const PView<T>& Pin, uint32_t p, bool need_jp, G2PIn<DIM, T>& in) {
 #pragma unroll
-  for (int d = 0; d < DIM; ++d) in.x[d] = Pin.x[(size_t)p * DIM + d];
+  for (int d = 0; d < DIM; ++d) in.x[d] = Pin.x[Pin.at(p, d, DIM)];
 #pragma unroll
-  for (int i = 0; i < DIM * DIM; ++i) in.F[i] = Pin.F[(size_t)p * DIM * DIM + i];
+  for (int i = 0; i < DIM * DIM; ++i) in.F[i] = Pin.F[Pin.at(p, i, DIM * DIM)];
   in.jp = need_jp ? Pin.Jp[p] : T(1);
 }
 
@@ -929,13 +959,13 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
   for (int d = 0; d < DIM; ++d) xn[d] = xp[d] + kp.dt * v[d];
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
-    Pout.x[(size_t)q * DIM + d] = xn[d];
-    Pout.v[(size_t)q * DIM + d] = v[d];
+    Pout.x[Pout.at(q, d, DIM)] = xn[d];
+    Pout.v[Pout.at(q, d, DIM)] = v[d];
   }
 #pragma unroll
   for (int i = 0; i < DD; ++i) {
-    Pout.C[(size_t)q * DD + i] = Cn[i];
-    Pout.F[(size_t)q * DD + i] = Fn[i];
+    Pout.C[Pout.at(q, i, DD)] = Cn[i];
+    Pout.F[Pout.at(q, i, DD)] = Fn[i];
   }
   if (write_jp) Pout.Jp[q] = jp_new;
   if (sorted) {
@@ -1070,16 +1100,16 @@ __global__ void __launch_bounds__(kThreads) k_diag(KParams<T> kp, PView<T> P, ui
     double v2 = 0;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-      const double vd = double(P.v[(size_t)p * DIM + d]);
+      const double vd = double(P.v[P.at(p, d, DIM)]);
       v2 += vd * vd;
       acc[3 + d] += m * vd;
     }
     acc[0] += 0.5 * m * v2;
-    acc[2] += -double(kp.gravity) * m * double(P.x[(size_t)p * DIM + 1]);
+    acc[2] += -double(kp.gravity) * m * double(P.x[P.at(p, 1, DIM)]);
     acc[6] += m;
     double F[DD];
 #pragma unroll
-    for (int i = 0; i < DD; ++i) F[i] = double(P.F[(size_t)p * DD + i]);
+    for (int i = 0; i < DD; ++i) F[i] = double(P.F[P.at(p, i, DD)]);
     double J, fr = 0;
     if constexpr (DIM == 3) {
       double R[9];

@@ -65,8 +65,10 @@ void sort_static(const ffmpm_params& p, const Layout& L, uint32_t* base, const v
   uint32_t* hist = vals1 + kStaticMaxN;
   // the array keeps the previous call's status word: start from zero
   cudaMemsetAsync(status, 0, sizeof(int32_t), s);
-  k_keys<DIM, T><<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kp, g, static_cast<const T*>(x), n, L.cell_bits,
-                                                                     keys_next, nullptr, status);
+  PView<T> xv{};
+  xv.x = static_cast<T*>(const_cast<void*>(x));
+  k_keys<DIM, T><<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kp, g, xv, n, L.cell_bits, keys_next, nullptr,
+                                                                     status);
   const uint32_t *ks = nullptr, *perm = nullptr;
   // 8-bit digits keep the histogram table inside the fixed array (256 x (tiles + 4) words)
   const int passes8 = (L.key_bits + 7) / 8;

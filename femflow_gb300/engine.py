@@ -100,9 +100,12 @@ def ptr(t) -> int:
     return 0 if t is None else t.data_ptr()
 
 
-def particles_struct(x, v, F, C, Jp, mass=None, mu_0=None, lambda_0=None) -> N.Particles:
+def particles_struct(x, v, F, C, Jp, mass=None, mu_0=None, lambda_0=None, stride: int = 0, n: int | None = None
+                     ) -> N.Particles:
+    """Row-major arrays (stride 0) or component-major arrays of the given stride (then pass n)."""
     s = N.Particles()
-    s.n = int(x.shape[0])
+    s.n = int(x.shape[0]) if n is None else int(n)
+    s.stride = int(stride)
     s.x, s.v, s.F, s.C = ptr(x), ptr(v), ptr(F), ptr(C)
     s.Jp = ptr(Jp)
     s.mass, s.mu_0, s.lambda_0 = ptr(mass), ptr(mu_0), ptr(lambda_0)

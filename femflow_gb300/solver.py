@@ -18,10 +18,14 @@ from . import engine as E
 
 
 class _Buffers:
+    """One particle state, component-major: x/v are [dim, n], F/C are [dim*dim, n] (row-major
+    matrix entries), so that every per-component access of a warp is coalesced."""
+
     def __init__(self, n, dim, dtype, device, per_particle_material):
         z = lambda *s: torch.empty(s, dtype=dtype, device=device)
-        self.x, self.v = z(n, dim), z(n, dim)
-        self.F, self.C = z(n, dim, dim), z(n, dim, dim)
+        self.n, self.dim = n, dim
+        self.x, self.v = z(dim, n), z(dim, n)
+        self.F, self.C = z(dim * dim, n), z(dim * dim, n)
         self.Jp = z(n)
         if per_particle_material:
             self.mass, self.mu_0, self.lambda_0 = z(n), z(n), z(n)
@@ -30,7 +34,14 @@ class _Buffers:
         self.ids = torch.empty(n, dtype=torch.int32, device=device)
 
     def struct(self) -> N.Particles:
-        return E.particles_struct(self.x, self.v, self.F, self.C, self.Jp, self.mass, self.mu_0, self.lambda_0)
+        return E.particles_struct(self.x, self.v, self.F, self.C, self.Jp, self.mass, self.mu_0, self.lambda_0,
+                                  stride=self.n, n=self.n)
+
+    def rows(self):
+        """The state as row-major (reference-layout) tensors, in buffer order."""
+        n, d = self.n, self.dim
+        return dict(x=self.x.T.contiguous(), v=self.v.T.contiguous(), F=self.F.T.reshape(n, d, d).contiguous(),
+                    C=self.C.T.reshape(n, d, d).contiguous(), Jp=self.Jp.clone())
 
 
 class MPMSolver:
@@ -59,10 +70,12 @@ class MPMSolver:
         self._a = _Buffers(n, dim, dtype, device, per_particle)
         self._b = _Buffers(n, dim, dtype, device, per_particle)
         a = self._a
-        a.x.copy_(x.to(device=device, dtype=dtype))
-        a.v.copy_(torch.zeros(n, dim) if v is None else torch.as_tensor(v).reshape(n, dim))
-        a.F.copy_(torch.eye(dim).expand(n, dim, dim) if F is None else torch.as_tensor(F).reshape(n, dim, dim))
-        a.C.copy_(torch.zeros(n, dim, dim) if C is None else torch.as_tensor(C).reshape(n, dim, dim))
+        a.x.copy_(x.to(device=device, dtype=dtype).T)
+        a.v.copy_((torch.zeros(n, dim) if v is None else torch.as_tensor(v).reshape(n, dim)).T)
+        Fr = torch.eye(dim).expand(n, dim, dim) if F is None else torch.as_tensor(F).reshape(n, dim, dim)
+        a.F.copy_(Fr.reshape(n, dim * dim).T)
+        Cr = torch.zeros(n, dim, dim) if C is None else torch.as_tensor(C).reshape(n, dim, dim)
+        a.C.copy_(Cr.reshape(n, dim * dim).T)
         a.Jp.copy_(torch.ones(n) if Jp is None else torch.as_tensor(Jp).reshape(n))
         if per_particle:
             a.mass.copy_(torch.as_tensor(mass).reshape(n))
@@ -142,16 +155,18 @@ class MPMSolver:
 
     # ------------------------------------------------------------------ state access
     def sorted_state(self):
+        """State in the current (block-sorted) buffer order, as row-major copies, with the ids."""
         c = self._cur
-        return dict(x=c.x, v=c.v, F=c.F, C=c.C, Jp=c.Jp, ids=c.ids, mass=c.mass, mu_0=c.mu_0, lambda_0=c.lambda_0)
+        out = c.rows()
+        out.update(ids=c.ids, mass=c.mass, mu_0=c.mu_0, lambda_0=c.lambda_0)
+        return out
 
     def state(self):
-        """State in the original particle order (a scatter by id; new tensors)."""
+        """State in the original particle order, row-major (new tensors)."""
         c = self._cur
         ids = c.ids.long()
         out = {}
-        for k in ("x", "v", "F", "C", "Jp"):
-            t = getattr(c, k)
+        for k, t in c.rows().items():
             o = torch.empty_like(t)
             o[ids] = t
             out[k] = o

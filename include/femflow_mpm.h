@@ -72,6 +72,10 @@ typedef struct ffmpm_particles {
   int64_t n;
   void *x, *v, *F, *C, *Jp;
   const void *mass, *mu_0, *lambda_0;
+  /* 0: the row-major layouts above.  > 0 (>= n): component-major — component c of particle p at
+   * [c * stride + p] (x, v: dim components; F, C: dim*dim, row-major within the matrix).  Lets a
+   * resident solver keep coalesced per-component arrays; the reference-facing calls use 0. */
+  int64_t stride;
 } ffmpm_particles;
 
 typedef struct ffmpm_grid {
