@@ -10,7 +10,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "../../include/femflow_mpm.h"
+#include "femflow_mpm.h"
 
 namespace ffmpm {
 

@@ -429,8 +429,35 @@ struct RecLayout {
   static_assert(kFloats == 1 + DIM + DIM * DIM + 3 * DIM, "record size");
 };
 
+// The state P2G reads of one particle (loaded ahead of the arithmetic so that the loads of
+// several particles are in flight together).
 template <int DIM, typename T>
-__device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>& g, const PView<T>& P, uint32_t p,
+struct P2GIn {
+  T x[DIM], v[DIM], F[DIM * DIM], C[DIM * DIM];
+  T m, mu0, lam0, jp;
+};
+
+template <int DIM, typename T>
+__device__ __forceinline__ void p2g_load(const KParams<T>& kp, const PView<T>& P, uint32_t p, P2GIn<DIM, T>& in) {
+  constexpr int DD = DIM * DIM;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    in.x[d] = P.x[P.at(p, d, DIM)];
+    in.v[d] = P.v[P.at(p, d, DIM)];
+  }
+#pragma unroll
+  for (int i = 0; i < DD; ++i) {
+    in.F[i] = P.F[P.at(p, i, DD)];
+    in.C[i] = P.C[P.at(p, i, DD)];
+  }
+  in.m = P.mass ? P.mass[p] : kp.mass;
+  in.mu0 = P.mu0 ? P.mu0[p] : kp.mu0;
+  in.lam0 = P.lam0 ? P.lam0[p] : kp.lam0;
+  in.jp = kp.model == FFMPM_MODEL_SNOW ? P.Jp[p] : T(1);
+}
+
+template <int DIM, typename T>
+__device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>& g, const P2GIn<DIM, T>& in,
                                            const int org[DIM], T* rec, int& cell, int32_t* status,
                                            uint32_t* fallbacks) {
   constexpr int DD = DIM * DIM;
@@ -440,7 +467,7 @@ __device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     int b;
-    ok = ok && base_of(P.x[P.at(p, d, DIM)], kp.inv_dx, kp.res, b, fx[d]);
+    ok = ok && base_of(in.x[d], kp.inv_dx, kp.res, b, fx[d]);
     lb[d] = b - org[d];
     ok = ok && lb[d] >= 0 && lb[d] + 2 < g.tile;
     T ww[3];
@@ -454,17 +481,10 @@ __device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>
     return false;
   }
   cell = DIM == 3 ? (lb[0] * g.bs + lb[1]) * g.bs + lb[2] : lb[0] * g.bs + lb[1];
-  T m, mu, lam;
-  lame_of(kp, P, p, m, mu, lam);
-  T F[DD], C[DD], A[DD], v[DIM];
-#pragma unroll
-  for (int i = 0; i < DD; ++i) {
-    F[i] = P.F[P.at(p, i, DD)];
-    C[i] = P.C[P.at(p, i, DD)];
-  }
-#pragma unroll
-  for (int d = 0; d < DIM; ++d) v[d] = P.v[P.at(p, d, DIM)];
-  affine_of<DIM, T>(kp, F, C, m, mu, lam, A, fallbacks);
+  const T m = in.m;
+  const T e = (kp.model == FFMPM_MODEL_SNOW) ? ffexp(kp.hardening * (T(1) - in.jp)) : kp.hardening;
+  T A[DD];
+  affine_of<DIM, T>(kp, in.F, in.C, m, in.mu0 * e, in.lam0 * e, A, fallbacks);
   const T dx = kp.dx;
   rec[0] = m;
 #pragma unroll
@@ -472,7 +492,7 @@ __device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>
     T af = T(0);
 #pragma unroll
     for (int c = 0; c < DIM; ++c) af += A[r * DIM + c] * fx[c];
-    rec[1 + r] = v[r] * m - dx * af;
+    rec[1 + r] = in.v[r] * m - dx * af;
   }
   constexpr int a0 = DIM == 3 ? 4 : 3;
 #pragma unroll
@@ -486,7 +506,7 @@ __device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>
 }
 
 template <int DIM, typename T, typename Sink>
-__global__ void __launch_bounds__(kThreads) k_p2g_cells(KParams<T> kp, Geom<DIM> g, PView<T> P,
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(KParams<T> kp, Geom<DIM> g, PView<T> P,
                                                         const uint32_t* __restrict__ perm,
                                                         const int4* __restrict__ chunks,
                                                         const WsHeader* __restrict__ hdr, Sink sink, int32_t* status,
@@ -524,17 +544,29 @@ __global__ void __launch_bounds__(kThreads) k_p2g_cells(KParams<T> kp, Geom<DIM>
 #pragma unroll
       for (int d = 0; d < DIM; ++d) org[d] = bc[d] * g.bs;
     }
-    // phase 1: one record per particle (cell -1 marks a particle that failed the bounds check)
-    for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {
-      T rec[RS];
-      int cell = -1;
-      if (!p2g_record<DIM, T>(kp, g, P, perm[ch.y + l], org, rec, cell, status, fallbacks)) cell = -1;
+    // phase 1: one record per particle (cell -1 marks a particle that failed the bounds check).
+    // Two particles per thread per iteration, both loaded before either is computed.
+    for (int l = threadIdx.x; l < ch.z; l += 2 * blockDim.x) {
+      const int l2 = l + blockDim.x;
+      const bool two = l2 < ch.z;
+      const uint32_t p1 = perm[ch.y + l], p2 = perm[ch.y + (two ? l2 : l)];
+      P2GIn<DIM, T> in[2];
+      p2g_load<DIM, T>(kp, P, p1, in[0]);
+      p2g_load<DIM, T>(kp, P, p2, in[1]);
 #pragma unroll
-      for (int i = RF; i < RS; ++i) rec[i] = T(0);
-      Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)l * RS);
+      for (int u = 0; u < 2; ++u) {
+        if (u == 1 && !two) break;
+        const int lu = u ? l2 : l;
+        T rec[RS];
+        int cell = -1;
+        if (!p2g_record<DIM, T>(kp, g, in[u], org, rec, cell, status, fallbacks)) cell = -1;
 #pragma unroll
-      for (int i = 0; i < RS / 4; ++i) dst[i] = Node4<T>{rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]};
-      cells[l] = cell;
+        for (int i = RF; i < RS; ++i) rec[i] = T(0);
+        Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)lu * RS);
+#pragma unroll
+        for (int i = 0; i < RS / 4; ++i) dst[i] = Node4<T>{rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]};
+        cells[lu] = cell;
+      }
     }
     __syncthreads();
     // phase 2: run heads (a particle whose cell differs from its predecessor's), compacted in
