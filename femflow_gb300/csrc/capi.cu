@@ -61,8 +61,8 @@ bool make_layout(const ffmpm_params& p, int64_t n, Layout* L) {
   L->cell_bits = p.dim * ilog2_ceil(L->bs);
   L->key_bits = ilog2_ceil(L->nblocks) + L->cell_bits;
   if (L->key_bits > 31) return false;
-  L->passes = std::max(1, (L->key_bits + kMaxDigitBits - 1) / kMaxDigitBits);
-  L->digit_bits = std::max(1, (L->key_bits + L->passes - 1) / L->passes);
+  L->passes = std::max(1, (L->key_bits + 7) / 8);
+  if (L->passes > kMaxRadixPasses) return false;
   L->n = n;
   L->ntiles = std::max<int64_t>(1, (n + kRadixTile - 1) / kRadixTile);
   L->max_chunks = (n + kChunk - 1) / kChunk + L->nblocks;
@@ -85,7 +85,7 @@ bool make_layout(const ffmpm_params& p, int64_t n, Layout* L) {
   L->off_keys1 = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
   L->off_vals0 = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
   L->off_vals1 = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
-  L->off_hist = take(sizeof(uint32_t) * (size_t(1) << L->digit_bits) * (L->ntiles + L->passes));
+  L->off_hist = take(sizeof(uint32_t) * radix_scratch_words(L->passes, L->ntiles));
   L->off_gridA = take(node_bytes * L->nnodes);
   L->off_gridB = take(node_bytes * L->nnodes);
   L->off_stage = take(p.deterministic ? node_bytes * tile_nodes * L->nblocks : 0);
@@ -287,8 +287,8 @@ void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const PV
   }
   const uint32_t* ks = nullptr;
   if (tm) tm->begin(1);
-  radix_sort(w.keys_next, n, L.passes, L.digit_bits, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, s, &ks, perm);
-  if (tm) tm->end(3 * L.passes);
+  radix_sort(w.keys_next, n, L.passes, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, &w.hdr->status, s, &ks, perm);
+  if (tm) tm->end(1 + L.passes);
   if (tm) tm->begin(2);
   k_plan<DIM><<<1, 1024, 0, s>>>(g, w.block_count, w.block_start, w.block_cnt, w.chunks, w.touched, w.occupied,
                                  w.hdr);
@@ -440,7 +440,7 @@ int op_sort(const ffmpm_params& p, const Layout& L, const Ws& w, const void* x, 
   k_keys<DIM, T><<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kp, g, xv, n, L.cell_bits, w.keys_next, nullptr,
                                                                      &w.hdr->status);
   const uint32_t *ks = nullptr, *perm = nullptr;
-  radix_sort(w.keys_next, n, L.passes, L.digit_bits, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, s, &ks, &perm);
+  radix_sort(w.keys_next, n, L.passes, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, &w.hdr->status, s, &ks, &perm);
   if (keys_out) cudaMemcpyAsync(keys_out, ks, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
   if (perm_out) cudaMemcpyAsync(perm_out, perm, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
   return check_launch();
@@ -598,7 +598,7 @@ int ffmpm_plan_info(const ffmpm_params* p, int64_t n, int64_t* info) {
   info[2] = L.nblocks;
   info[3] = L.key_bits;
   info[4] = L.passes;
-  info[5] = 3 * L.passes + 4;  // radix passes x (hist, scan, scatter) + plan + P2G + grid + G2P
+  info[5] = L.passes + 5;  // digit histogram + one kernel per radix pass + plan + P2G + grid + G2P
   info[6] = L.tile;
   info[7] = L.max_chunks;
   return FFMPM_OK;

@@ -28,7 +28,7 @@ static_assert(sizeof(WsHeader) == 256, "header is one 256-byte line");
 // Offsets (bytes) of every region of a workspace, derived from (params, n).
 struct Layout {
   int dim = 3, real_bytes = 4, res = 0, R = 0, bs = 0, nb = 0, tile = 0;
-  int key_bits = 0, passes = 0, digit_bits = 8, cell_bits = 0;
+  int key_bits = 0, passes = 0, cell_bits = 0;
   int64_t n = 0, nblocks = 0, nnodes = 0, max_chunks = 0, ntiles = 0;
   size_t off_block_count = 0, off_block_start = 0, off_block_cnt = 0, off_chunks = 0, off_touched = 0,
          off_occupied = 0, off_keys_next = 0, off_keys0 = 0, off_keys1 = 0, off_vals0 = 0, off_vals1 = 0,
@@ -39,12 +39,13 @@ bool make_layout(const ffmpm_params& p, int64_t n, Layout* L);
 
 int sm_count();
 
-// Radix sort (sort.cu).  Sorts `passes` digits of `digit_bits` (<= 11) bits of keys_in (n keys);
-// values start as the identity permutation.  `hist` holds (1 << digit_bits) * (ntiles + passes)
-// words.  Returns the buffers that hold the sorted keys / permutation.
-constexpr int kMaxDigitBits = 11;
-void radix_sort(const uint32_t* keys_in, uint32_t n, int passes, int digit_bits, uint32_t* keys0, uint32_t* keys1,
-                uint32_t* vals0, uint32_t* vals1, uint32_t* hist, int ntiles, cudaStream_t s,
+// Radix sort (sort.cu): stable, 8-bit digits, `passes` passes over keys_in (n keys); values start
+// as the identity permutation.  `scratch` holds radix_scratch_words(passes, ntiles) words (zeroed
+// by the call).  Returns the buffers that hold the sorted keys / permutation.
+constexpr int kMaxRadixPasses = 4;
+size_t radix_scratch_words(int passes, int64_t ntiles);
+void radix_sort(const uint32_t* keys_in, uint32_t n, int passes, uint32_t* keys0, uint32_t* keys1, uint32_t* vals0,
+                uint32_t* vals1, uint32_t* scratch, int ntiles, int32_t* status, cudaStream_t s,
                 const uint32_t** keys_sorted, const uint32_t** perm);
 
 }  // namespace ffmpm

@@ -17,10 +17,11 @@ namespace {
 
 constexpr int64_t kStaticMaxN = FFMPM_STATIC_SORT_MAX_N;
 constexpr int64_t kStaticTiles = (kStaticMaxN + kRadixTile - 1) / kRadixTile;
-// [status word + pad: 64 words][keys_next][keys0][keys1][vals0][vals1][histograms 256 x tiles]
-// [digit totals 256 x 4 passes]
+// [status word + pad: 64 words][keys_next][keys0][keys1][vals0][vals1][radix scratch of 4 passes:
+// digit histograms, tile counters, look-back words 256 x tiles]
 constexpr size_t kHeaderWords = 64;
-constexpr size_t kStaticWords = kHeaderWords + 5 * size_t(kStaticMaxN) + 256 * size_t(kStaticTiles + 4);
+constexpr size_t kRadixWords = size_t(kMaxRadixPasses) * (256 + 32 + 256 * size_t(kStaticTiles));
+constexpr size_t kStaticWords = kHeaderWords + 5 * size_t(kStaticMaxN) + kRadixWords;
 
 __device__ __align__(256) uint32_t g_sort_scratch[kStaticWords];
 
@@ -70,10 +71,7 @@ void sort_static(const ffmpm_params& p, const Layout& L, uint32_t* base, const v
   k_keys<DIM, T><<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kp, g, xv, n, L.cell_bits, keys_next, nullptr,
                                                                      status);
   const uint32_t *ks = nullptr, *perm = nullptr;
-  // 8-bit digits keep the histogram table inside the fixed array (256 x (tiles + 4) words)
-  const int passes8 = (L.key_bits + 7) / 8;
-  radix_sort(keys_next, n, passes8 > 0 ? passes8 : 1, 8, keys0, keys1, vals0, vals1, hist, (int)L.ntiles, s, &ks,
-             &perm);
+  radix_sort(keys_next, n, L.passes, keys0, keys1, vals0, vals1, hist, (int)L.ntiles, status, s, &ks, &perm);
   if (keys_out) cudaMemcpyAsync(keys_out, ks, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
   if (perm_out) cudaMemcpyAsync(perm_out, perm, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
 }

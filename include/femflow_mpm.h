@@ -151,7 +151,7 @@ int ffmpm_plan_info(const ffmpm_params *p, int64_t n, int64_t *info);
 /* The block sort of ffmpm_sort_by_block (same keys, same stable permutation) without a workspace
  * and without any device allocation.  It is meant for callers that cannot allocate device memory:
  * a host application that owns every GPU allocation and hands its plugins device pointers only,
- * or a real-time loop that forbids allocation once it has started.  The scratch (about 5.3 MB:
+ * or a real-time loop that forbids allocation once it has started.  The scratch (about 5.5 MB:
  * five n-sized key/index arrays plus the digit histograms) is one static array in this library,
  * which every GPU that loads the library keeps until the process exits.
  *   - n must be <= FFMPM_STATIC_SORT_MAX_N, otherwise FFMPM_ERR_CAPACITY and nothing runs.
