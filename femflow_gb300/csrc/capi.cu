@@ -336,6 +336,26 @@ void launch_p2g(const ffmpm_params& p, const Layout& L, const Ws& w, const PView
 }
 
 template <int DIM, typename T>
+void launch_p2g_det(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<T>& P, const uint32_t* perm,
+                    cudaStream_t s) {
+  const int tn = DIM == 3 ? L.tile * L.tile * L.tile : L.tile * L.tile;
+  const size_t smem = p2g_det_smem_bytes<DIM, T>(tn);
+  auto kern = k_p2g_det<DIM, T>;
+  set_smem(kern, smem);
+  kern<<<work_grid(L.nblocks, resident_per_sm(kern, smem)), kThreads, smem, s>>>(
+      kparams<T>(p), geom<DIM>(L), P, perm, w.occupied, w.hdr, static_cast<Node4<T>*>(w.stage), &w.hdr->status,
+      &w.hdr->polar_fallbacks);
+}
+
+template <int DIM, typename T>
+void launch_grid_update_det(const ffmpm_params& p, const Layout& L, const Ws& w, cudaStream_t s, T* user_gv = nullptr,
+                            T* user_gm = nullptr) {
+  k_grid_update_det<DIM, T><<<work_grid(L.nblocks, 8), kThreads, 0, s>>>(
+      kparams<T>(p), geom<DIM>(L), w.touched, w.block_cnt, w.hdr, static_cast<const Node4<T>*>(w.stage),
+      static_cast<Node4<T>*>(w.gridB), user_gv, user_gm);
+}
+
+template <int DIM, typename T>
 void launch_grid_update(const ffmpm_params& p, const Layout& L, const Ws& w, cudaStream_t s) {
   k_grid_update<DIM, T><<<work_grid(L.nblocks, 8), kThreads, 0, s>>>(
       kparams<T>(p), geom<DIM>(L), w.touched, w.hdr, static_cast<Node4<T>*>(w.gridA), static_cast<Node4<T>*>(w.gridB));
@@ -361,8 +381,13 @@ int op_substep(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_partic
   const PView<T> pv = pview<T>(*P);
   const uint32_t* perm = nullptr;
   sort_and_plan<DIM, T>(p, L, w, pv, false, &perm, s);
-  launch_p2g<DIM, T>(p, L, w, pv, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s);
-  launch_grid_update<DIM, T>(p, L, w, s);
+  if (p.deterministic) {
+    launch_p2g_det<DIM, T>(p, L, w, pv, perm, s);
+    launch_grid_update_det<DIM, T>(p, L, w, s);
+  } else {
+    launch_p2g<DIM, T>(p, L, w, pv, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s);
+    launch_grid_update<DIM, T>(p, L, w, s);
+  }
   G2PExtra ex{};
   int rc = launch_g2p<DIM, T, true, false>(p, L, w, pv, pv, perm, nullptr, ex, s);
   return rc != FFMPM_OK ? rc : check_launch();
@@ -380,10 +405,16 @@ int op_substeps_sorted(const ffmpm_params& p, const Layout& L, const Ws& w, ffmp
     const uint32_t* perm = nullptr;
     sort_and_plan<DIM, T>(p, L, w, in, k > 0, &perm, s, tm);
     if (tm) tm->begin(3);
-    launch_p2g<DIM, T>(p, L, w, in, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s);
+    if (p.deterministic)
+      launch_p2g_det<DIM, T>(p, L, w, in, perm, s);
+    else
+      launch_p2g<DIM, T>(p, L, w, in, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s);
     if (tm) tm->end(1);
     if (tm) tm->begin(4);
-    launch_grid_update<DIM, T>(p, L, w, s);
+    if (p.deterministic)
+      launch_grid_update_det<DIM, T>(p, L, w, s);
+    else
+      launch_grid_update<DIM, T>(p, L, w, s);
     if (tm) tm->end(1);
     G2PExtra ex{ids_in, ids_out, w.keys_next, w.block_count, L.cell_bits};
     if (tm) tm->begin(5);
@@ -403,8 +434,13 @@ int op_p2g(const ffmpm_params& p, const Layout& L, const Ws& w, const ffmpm_part
   const PView<T> pv = pview<T>(*P);
   const uint32_t* perm = nullptr;
   sort_and_plan<DIM, T>(p, L, w, pv, false, &perm, s);
-  launch_p2g<DIM, T>(p, L, w, pv, perm, UserSink<T, DIM>{static_cast<T*>(grid->velocity), static_cast<T*>(grid->mass)},
-                     s);
+  if (p.deterministic) {
+    launch_p2g_det<DIM, T>(p, L, w, pv, perm, s);
+    launch_grid_update_det<DIM, T>(p, L, w, s, static_cast<T*>(grid->velocity), static_cast<T*>(grid->mass));
+  } else {
+    launch_p2g<DIM, T>(p, L, w, pv, perm,
+                       UserSink<T, DIM>{static_cast<T*>(grid->velocity), static_cast<T*>(grid->mass)}, s);
+  }
   return check_launch();
 }
 
@@ -501,7 +537,13 @@ bool supported(const ffmpm_params& p) {
 int prologue(const ffmpm_params* p, int64_t n, void* ws, size_t ws_bytes, Layout* L) {
   if (!p || !make_layout(*p, n, L)) return FFMPM_ERR_BADARG;
   if (!supported(*p)) return FFMPM_ERR_UNSUPPORTED;
-  if (p->deterministic) return FFMPM_ERR_UNSUPPORTED;
+  if (p->deterministic) {
+    const int tn = p->dim == 3 ? L->tile * L->tile * L->tile : L->tile * L->tile;
+    const size_t smem = p->real_bytes == 4 ? (p->dim == 3 ? p2g_det_smem_bytes<3, float>(tn) : p2g_det_smem_bytes<2, float>(tn))
+                                           : (p->dim == 3 ? p2g_det_smem_bytes<3, double>(tn)
+                                                          : p2g_det_smem_bytes<2, double>(tn));
+    if (smem > 200 * 1024) return FFMPM_ERR_UNSUPPORTED;  // warp tiles + records must fit in shared memory
+  }
   if (!ws || ws_bytes < L->total || (reinterpret_cast<uintptr_t>(ws) & 255)) return FFMPM_ERR_WORKSPACE;
   return FFMPM_OK;
 }

@@ -695,6 +695,210 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
   }
 }
 
+// ----------------------------------------------------------------------------------------------
+// Deterministic P2G.  One CTA per occupied block.  Runs (as in k_p2g_cells) go to warps by a fixed
+// rule (run r of a chunk -> warp r mod 8) and every warp adds its runs' node sums, in run order,
+// into its own shared tile without atomics; the eight tiles are summed in warp order into the
+// block's staging tile.  The grid update then sums the (at most 2^DIM) staged tiles that cover a
+// node in a fixed block order.  Every floating-point sum therefore has a fixed order and the
+// result is bit-identical from run to run.
+template <int DIM, typename T>
+__host__ __device__ constexpr size_t p2g_det_smem_bytes(int TN) {
+  return size_t(kThreads / 32) * 4 * TN * sizeof(T) + size_t(kChunk) * RecLayout<DIM>::kStride * sizeof(T) +
+         sizeof(int) * (2 * kChunk + 1);
+}
+
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kThreads) k_p2g_det(KParams<T> kp, Geom<DIM> g, PView<T> P,
+                                                      const uint32_t* __restrict__ perm,
+                                                      const int4* __restrict__ occupied,
+                                                      const WsHeader* __restrict__ hdr, Node4<T>* __restrict__ stage,
+                                                      int32_t* status, uint32_t* fallbacks) {
+  constexpr int RF = RecLayout<DIM>::kFloats;
+  constexpr int RS = RecLayout<DIM>::kStride;
+  constexpr int NW = kThreads / 32;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int TN = tile_nodes<DIM>(g);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* wtiles = reinterpret_cast<T*>(smem_raw);           // [NW][4][TN]
+  T* recs = wtiles + (size_t)NW * 4 * TN;                // [kChunk][RS]
+  int* cells = reinterpret_cast<int*>(recs + (size_t)kChunk * RS);
+  int* runs = cells + kChunk;                            // [kChunk + 1]
+  __shared__ int nruns_s;
+  __shared__ int warp_cnt[kThreads / 32];
+  T* mytile = wtiles + (size_t)warp * 4 * TN;
+  const int T1 = g.tile;
+  constexpr int LP = DIM == 3 ? 9 : 3;
+  constexpr int NG = 32 / LP;
+  const int grp = lane / LP;
+  const int jk = lane - grp * LP;
+  const bool active = grp < NG;
+  const int oj = DIM == 3 ? jk / 3 : jk, ok = DIM == 3 ? jk % 3 : 0;
+  constexpr int a0 = 1 + DIM;
+  constexpr int w0 = RecLayout<DIM>::kW;
+  const uint32_t nocc = hdr->n_occupied;
+  for (uint32_t ob = blockIdx.x; ob < nocc; ob += gridDim.x) {
+    const int4 occ = occupied[ob];
+    int org[DIM];
+    {
+      int bc[DIM];
+      block_coords<DIM>(g, occ.x, bc);
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) org[d] = bc[d] * g.bs;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < NW * 4 * TN; t += blockDim.x) wtiles[t] = T(0);
+    for (int c0 = 0; c0 < occ.z; c0 += kChunk) {
+      const int cz = min(kChunk, occ.z - c0);
+      const uint32_t s0 = (uint32_t)(occ.y + c0);
+      __syncthreads();  // tiles zeroed / previous chunk's records consumed
+      for (int l = threadIdx.x; l < cz; l += 2 * blockDim.x) {
+        const int l2 = l + blockDim.x;
+        const bool two = l2 < cz;
+        const uint32_t p1 = perm[s0 + l], p2 = perm[s0 + (two ? l2 : l)];
+        P2GIn<DIM, T> in[2];
+        p2g_load<DIM, T>(kp, P, p1, in[0]);
+        p2g_load<DIM, T>(kp, P, p2, in[1]);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          if (u == 1 && !two) break;
+          const int lu = u ? l2 : l;
+          T rec[RS];
+          int cell = -1;
+          if (!p2g_record<DIM, T>(kp, g, in[u], org, rec, cell, status, fallbacks)) cell = -1;
+#pragma unroll
+          for (int i = RF; i < RS; ++i) rec[i] = T(0);
+          Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)lu * RS);
+#pragma unroll
+          for (int i = 0; i < RS / 4; ++i) dst[i] = Node4<T>{rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]};
+          cells[lu] = cell;
+        }
+      }
+      __syncthreads();
+      {
+        const int per_t = (cz + blockDim.x - 1) / blockDim.x;
+        const int beg = threadIdx.x * per_t;
+        int heads = 0;
+        for (int l = beg; l < min(cz, beg + per_t); ++l) heads += (l == 0 || cells[l] != cells[l - 1]);
+        int inc = heads;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, inc, o);
+          if (lane >= o) inc += t;
+        }
+        if (lane == 31) warp_cnt[warp] = inc;
+        __syncthreads();
+        int before = 0, tot = 0;
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) {
+          before += w < warp ? warp_cnt[w] : 0;
+          tot += warp_cnt[w];
+        }
+        int r = before + inc - heads;
+        for (int l = beg; l < min(cz, beg + per_t); ++l)
+          if (l == 0 || cells[l] != cells[l - 1]) runs[r++] = l;
+        if (threadIdx.x == 0) {
+          nruns_s = tot;
+          runs[tot] = cz;
+        }
+      }
+      __syncthreads();
+      const int nruns = nruns_s;
+      for (int r = warp; r < nruns; r += NW) {
+        const int l0 = runs[r], l1 = runs[r + 1];
+        const int cl = cells[l0];
+        if (cl < 0) continue;
+        T acc[3][4];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = T(0);
+        if (active) {
+          for (int l = l0 + grp; l < l1; l += NG) {
+            const Node4<T>* src = reinterpret_cast<const Node4<T>*>(recs + (size_t)l * RS);
+            T rv[RS];
+#pragma unroll
+            for (int i = 0; i < (RF + 3) / 4; ++i) {
+              const Node4<T> q4 = src[i];
+              rv[4 * i] = q4.x;
+              rv[4 * i + 1] = q4.y;
+              rv[4 * i + 2] = q4.z;
+              rv[4 * i + 3] = q4.w;
+            }
+            const T m = rv[0];
+            T wjk;
+            if constexpr (DIM == 3) {
+              const T wy = oj == 0 ? rv[w0 + 3] : (oj == 1 ? rv[w0 + 4] : rv[w0 + 5]);
+              const T wz = ok == 0 ? rv[w0 + 6] : (ok == 1 ? rv[w0 + 7] : rv[w0 + 8]);
+              wjk = wy * wz;
+            } else {
+              wjk = oj == 0 ? rv[w0 + 3] : (oj == 1 ? rv[w0 + 4] : rv[w0 + 5]);
+            }
+            T bse[DIM], stp[DIM];
+#pragma unroll
+            for (int rr = 0; rr < DIM; ++rr) {
+              T b = rv[1 + rr] + rv[a0 + rr * DIM + 1] * T(oj);
+              if constexpr (DIM == 3) b += rv[a0 + rr * DIM + 2] * T(ok);
+              bse[rr] = b;
+              stp[rr] = rv[a0 + rr * DIM];
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+              const T wgt = rv[w0 + i] * wjk;
+#pragma unroll
+              for (int rr = 0; rr < DIM; ++rr) acc[i][rr] += wgt * (bse[rr] + T(i) * stp[rr]);
+              acc[i][3] += wgt * m;
+            }
+          }
+        }
+#pragma unroll
+        for (int off = 1; off < NG; off <<= 1) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) {
+              const T t = __shfl_down_sync(0xffffffffu, acc[i][cc], off * LP);
+              if (grp % (2 * off) == 0 && grp + off < NG) acc[i][cc] += t;
+            }
+        }
+        if (grp == 0) {
+          int lb[DIM];
+          if constexpr (DIM == 3) {
+            lb[2] = cl % g.bs;
+            lb[1] = (cl / g.bs) % g.bs;
+            lb[0] = cl / (g.bs * g.bs);
+          } else {
+            lb[1] = cl % g.bs;
+            lb[0] = cl / g.bs;
+          }
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            const int idx = DIM == 3 ? ((lb[0] + i) * T1 + lb[1] + oj) * T1 + lb[2] + ok : (lb[0] + i) * T1 + lb[1] + oj;
+            mytile[idx] += acc[i][0];
+            mytile[TN + idx] += acc[i][1];
+            if constexpr (DIM == 3) mytile[2 * TN + idx] += acc[i][2];
+            mytile[3 * TN + idx] += acc[i][3];
+          }
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    // the block's staging tile: warp tiles summed in warp order
+    Node4<T>* st = stage + (size_t)occ.x * TN;
+    for (int t = threadIdx.x; t < TN; t += blockDim.x) {
+      T a = T(0), b = T(0), c = T(0), m = T(0);
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        const T* wt = wtiles + (size_t)w * 4 * TN;
+        a += wt[t];
+        b += wt[TN + t];
+        c += wt[2 * TN + t];
+        m += wt[3 * TN + t];
+      }
+      st[t] = Node4<T>{a, b, c, m};
+    }
+  }
+}
+
 template <int DIM, typename T, typename Sink, bool kDirect>
 __global__ void __launch_bounds__(kThreads) k_p2g(KParams<T> kp, Geom<DIM> g, PView<T> P,
                                                   const uint32_t* __restrict__ perm, const int4* __restrict__ chunks,
@@ -822,6 +1026,79 @@ __global__ void __launch_bounds__(kThreads) k_grid_update(KParams<T> kp, Geom<DI
       grid_node<DIM, T>(kp, I, vel, a.w);
       B[node] = Node4<T>{vel[0], vel[1], vel[2], a.w};
       A[node] = Node4<T>{T(0), T(0), T(0), T(0)};
+    }
+  }
+}
+
+// Grid update of the deterministic mode: node momentum/mass = staged tiles of the blocks whose
+// tiles cover the node, summed in a fixed order; then the grid rule (grid_node).
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kThreads) k_grid_update_det(KParams<T> kp, Geom<DIM> g,
+                                                              const uint32_t* __restrict__ touched,
+                                                              const uint32_t* __restrict__ block_cnt,
+                                                              const WsHeader* __restrict__ hdr,
+                                                              const Node4<T>* __restrict__ stage,
+                                                              Node4<T>* __restrict__ B, T* user_gv, T* user_gm) {
+  const uint32_t nt = hdr->n_touched;
+  const int per_block = DIM == 3 ? g.bs * g.bs * g.bs : g.bs * g.bs;
+  const int TN = tile_nodes<DIM>(g);
+  const int T1 = g.tile;
+  for (uint32_t tb = blockIdx.x; tb < nt; tb += gridDim.x) {
+    int bc[DIM];
+    block_coords<DIM>(g, (int)touched[tb], bc);
+    for (int t = threadIdx.x; t < per_block; t += blockDim.x) {
+      int loc[DIM], I[DIM];
+      if constexpr (DIM == 3) {
+        loc[0] = t / (g.bs * g.bs);
+        loc[1] = (t / g.bs) % g.bs;
+        loc[2] = t % g.bs;
+      } else {
+        loc[0] = t / g.bs;
+        loc[1] = t % g.bs;
+      }
+      bool in = true;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        I[d] = bc[d] * g.bs + loc[d];
+        in = in && I[d] < g.R;
+      }
+      if (!in) continue;
+      T a = T(0), b = T(0), c = T(0), m = T(0);
+#pragma unroll
+      for (int o = 0; o < (1 << DIM); ++o) {
+        int src[DIM], tl[DIM];
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const int od = (o >> (DIM - 1 - d)) & 1;
+          src[d] = bc[d] - od;
+          tl[d] = loc[d] + od * g.bs;
+          ok = ok && src[d] >= 0 && tl[d] < T1;
+        }
+        if (!ok) continue;
+        int sb = 0;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) sb = sb * g.nb + src[d];
+        if (block_cnt[sb] == 0) continue;
+        const int ti = DIM == 3 ? (tl[0] * T1 + tl[1]) * T1 + tl[2] : tl[0] * T1 + tl[1];
+        const Node4<T> v = stage[(size_t)sb * TN + ti];
+        a += v.x;
+        b += v.y;
+        c += v.z;
+        m += v.w;
+      }
+      const int64_t node = node_index<DIM>(g.R, I);
+      if (user_gv) {
+        // per-phase API: add the deterministic node sums into the caller's grid
+        user_gv[node * DIM + 0] += a;
+        user_gv[node * DIM + 1] += b;
+        if constexpr (DIM == 3) user_gv[node * DIM + 2] += c;
+        user_gm[node] += m;
+      } else {
+        T vel[3] = {a, b, c};
+        grid_node<DIM, T>(kp, I, vel, m);
+        B[node] = Node4<T>{vel[0], vel[1], vel[2], m};
+      }
     }
   }
 }

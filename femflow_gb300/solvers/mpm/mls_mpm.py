@@ -23,7 +23,7 @@ def make_mls_mpm_coefficients(lenx: int, dim: int, dtype=torch.float32, device="
 
 
 def solve_mls_mpm_3d(res, inv_dx, hardening, dx, dt, volume, gravity, particles, v, F, C, Jp, *,
-                     check: bool = True):
+                     check: bool = True, deterministic: bool = False):
     """mls_mpm.py:40-79: one substep (p2g, grid_op, g2p on a fresh (res+1)^3 grid), in place.
 
     ``particles`` is a ``ParticleSet`` (or a list of ``Particle``, converted on the host).  The
@@ -35,7 +35,8 @@ def solve_mls_mpm_3d(res, inv_dx, hardening, dx, dt, volume, gravity, particles,
     st = E.stage([pset.pos, pset.mass, pset.mu_0, pset.lambda_0, v, F, C, Jp], dtype=dtype)
     x, m, mu, lam, vv, FF, CC, JJ = st.dev
     E.check_tensors(dtype, x, m, mu, lam, vv, FF, CC, JJ)
-    prm = E.make_params(3, res, dtype, dx, inv_dx, dt, gravity, volume, hardening, model="neo_hookean")
+    prm = E.make_params(3, res, dtype, dx, inv_dx, dt, gravity, volume, hardening, model="neo_hookean",
+                        deterministic=deterministic)
     ps = E.particles_struct(x, vv, FF, CC, JJ, m, mu, lam)
     P.run("ffmpm_substep", prm, ps.n, x.device, ctypes.byref(prm), ctypes.byref(ps), check=check)
     st.write_back([0, 4, 5, 6, 7])

@@ -14,15 +14,19 @@ from . import _phase as P
 
 
 def p2g(inv_dx, hardening, dx, dt, volume, grid_velocity, grid_mass, particles, v, F, C, Jp,
-        model: str = "neo_hookean"):
-    """three_d/p2g.py:14-80: add the particles' momentum and mass into the grid."""
+        model: str = "neo_hookean", *, deterministic: bool = False):
+    """three_d/p2g.py:14-80: add the particles' momentum and mass into the grid.
+
+    ``deterministic=True`` sums every node in a fixed order (bit-identical across runs).
+    """
     pset, plist = P.split_particles(particles)
     dtype = P.dtype_of(v, F, grid_velocity)
     st = E.stage([pset.pos, pset.mass, pset.mu_0, pset.lambda_0, v, F, C, Jp, grid_velocity, grid_mass], dtype=dtype)
     x, m, mu, lam, vv, FF, CC, JJ, gv, gm = st.dev
     E.check_tensors(dtype, x, m, mu, lam, vv, FF, CC, JJ, gv, gm)
     res = gv.shape[0] - 1
-    prm = E.make_params(3, res, dtype, dx, inv_dx, dt, 0.0, volume, hardening, model=model)
+    prm = E.make_params(3, res, dtype, dx, inv_dx, dt, 0.0, volume, hardening, model=model,
+                        deterministic=deterministic)
     ps = E.particles_struct(x, vv, FF, CC, JJ, m, mu, lam)
     g = E.grid_struct(gv, gm)
     P.run("ffmpm_p2g", prm, ps.n, x.device, ctypes.byref(prm), ctypes.byref(ps), ctypes.byref(g))

@@ -15,14 +15,15 @@ from . import _phase as P
 
 
 def p2g(inv_dx, hardening, mu_0, lambda_0, mass, dx, dt, volume, grid_velocity, grid_mass, x, v, F, C, Jp,
-        model: str = "neo_hookean"):
-    """two_d/p2g.py:11-76."""
+        model: str = "neo_hookean", *, deterministic: bool = False):
+    """two_d/p2g.py:11-76 (``deterministic=True``: fixed summation order, bit-identical runs)."""
     dtype = P.dtype_of(x, v, grid_velocity)
     st = E.stage([x, v, F, C, Jp, grid_velocity, grid_mass], dtype=dtype)
     xx, vv, FF, CC, JJ, gv, gm = st.dev
     E.check_tensors(dtype, xx, vv, FF, CC, JJ, gv, gm)
     res = gv.shape[0] - 1
-    prm = E.make_params(2, res, dtype, dx, inv_dx, dt, 0.0, volume, hardening, mass, mu_0, lambda_0, model=model)
+    prm = E.make_params(2, res, dtype, dx, inv_dx, dt, 0.0, volume, hardening, mass, mu_0, lambda_0, model=model,
+                        deterministic=deterministic)
     ps = E.particles_struct(xx, vv, FF, CC, JJ)
     g = E.grid_struct(gv, gm)
     P.run("ffmpm_p2g", prm, ps.n, xx.device, ctypes.byref(prm), ctypes.byref(ps), ctypes.byref(g))
@@ -57,7 +58,7 @@ def g2p(inv_dx, dt, grid_velocity, x, v, F, C, Jp, model: str = "neo_hookean"):
 
 
 def solve_mls_mpm_2d(res, inv_dx, hardening, mu_0, lambda_0, mass, dx, dt, volume, gravity, x, v, F, C, Jp,
-                     model: str = "neo_hookean", wall_mode: str = "reference"):
+                     model: str = "neo_hookean", wall_mode: str = "reference", *, deterministic: bool = False):
     """One 2D substep: the p2g -> grid_op -> g2p sequence on a fresh grid, fused on the GPU.
 
     The reference has no 2D driver; this is the call sequence of mls_mpm.py:54-79 with the
@@ -68,7 +69,7 @@ def solve_mls_mpm_2d(res, inv_dx, hardening, mu_0, lambda_0, mass, dx, dt, volum
     xx, vv, FF, CC, JJ = st.dev
     E.check_tensors(dtype, xx, vv, FF, CC, JJ)
     prm = E.make_params(2, res, dtype, dx, inv_dx, dt, gravity, volume, hardening, mass, mu_0, lambda_0,
-                        model=model, wall_mode=wall_mode)
+                        model=model, wall_mode=wall_mode, deterministic=deterministic)
     ps = E.particles_struct(xx, vv, FF, CC, JJ)
     P.run("ffmpm_substep", prm, ps.n, xx.device, ctypes.byref(prm), ctypes.byref(ps))
     st.write_back([0, 1, 2, 3, 4])
