@@ -529,10 +529,7 @@ bool particles_ok(const ffmpm_params& p, const ffmpm_particles* P, bool need_jp)
   return true;
 }
 
-bool supported(const ffmpm_params& p) {
-  // 3D snow needs a device 3x3 SVD with clamping in G2P (three_d/g2p.py:48-58); not built.
-  return !(p.dim == 3 && p.model == FFMPM_MODEL_SNOW);
-}
+bool supported(const ffmpm_params& p) { return true; }
 
 int prologue(const ffmpm_params* p, int64_t n, void* ws, size_t ws_bytes, Layout* L) {
   if (!p || !make_layout(*p, n, L)) return FFMPM_ERR_BADARG;

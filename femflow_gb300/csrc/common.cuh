@@ -205,6 +205,88 @@ __device__ __forceinline__ void polar3(const T F[9], T R[9], uint32_t* fallbacks
   }
 }
 
+// 3x3 SVD F = U diag(s) V^T, s >= 0 descending, by one-sided (Hestenes) Jacobi rotations of the
+// columns of F; U and V are orthogonal (det U det V = sign det F).  Used by the snow model's
+// singular-value clamp (three_d/g2p.py:48-58).
+template <typename T>
+__device__ __forceinline__ void svd3(const T F[9], T U[9], T s[3], T V[9]) {
+  T A[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    A[i] = F[i];
+    V[i] = (i % 4 == 0) ? T(1) : T(0);
+  }
+  const T tol = T(4) * Eps<T>::value;
+  for (int sweep = 0; sweep < 12; ++sweep) {
+    T off = T(0);
+#pragma unroll
+    for (int pi = 0; pi < 3; ++pi) {
+      const int p = pi == 2 ? 1 : 0, q = pi == 0 ? 1 : 2;
+      T alpha = 0, beta = 0, gamma = 0;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        alpha += A[i * 3 + p] * A[i * 3 + p];
+        beta += A[i * 3 + q] * A[i * 3 + q];
+        gamma += A[i * 3 + p] * A[i * 3 + q];
+      }
+      const T nrm = ffsqrt(alpha * beta);
+      if (!(nrm > T(0)) || gamma == T(0)) continue;
+      const T rel = ffabs(gamma) / nrm;
+      off = rel > off ? rel : off;
+      if (rel < tol) continue;
+      const T zeta = (beta - alpha) / (T(2) * gamma);
+      const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (ffabs(zeta) + ffsqrt(T(1) + zeta * zeta));
+      const T c = T(1) / ffsqrt(T(1) + tt * tt), sn = c * tt;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const T ap = A[i * 3 + p], aq = A[i * 3 + q];
+        A[i * 3 + p] = c * ap - sn * aq;
+        A[i * 3 + q] = sn * ap + c * aq;
+        const T vp = V[i * 3 + p], vq = V[i * 3 + q];
+        V[i * 3 + p] = c * vp - sn * vq;
+        V[i * 3 + q] = sn * vp + c * vq;
+      }
+    }
+    if (off < tol) break;
+  }
+  T n[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) n[j] = ffsqrt(A[j] * A[j] + A[3 + j] * A[3 + j] + A[6 + j] * A[6 + j]);
+  // order the columns by decreasing singular value (three compare-and-swap steps)
+#pragma unroll
+  for (int step = 0; step < 3; ++step) {
+    const int a = step == 1 ? 1 : 0, b = step == 0 ? 1 : 2;
+    if (n[b] > n[a]) {
+      const T tn = n[a];
+      n[a] = n[b];
+      n[b] = tn;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        T t1 = A[i * 3 + a];
+        A[i * 3 + a] = A[i * 3 + b];
+        A[i * 3 + b] = t1;
+        t1 = V[i * 3 + a];
+        V[i * 3 + a] = V[i * 3 + b];
+        V[i * 3 + b] = t1;
+      }
+    }
+  }
+  const T smax = n[0] > T(0) ? n[0] : T(1);
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    s[j] = n[j];
+    const bool full = n[j] > smax * T(64) * Eps<T>::value;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) U[i * 3 + j] = full ? A[i * 3 + j] / n[j] : T(0);
+  }
+  // a (numerically) null third column: complete U with the cross product of the first two
+  if (!(n[2] > smax * T(64) * Eps<T>::value)) {
+    U[2] = U[3] * U[7] - U[6] * U[4];
+    U[5] = U[6] * U[1] - U[0] * U[7];
+    U[8] = U[0] * U[4] - U[3] * U[1];
+  }
+}
+
 // linear_algebra.py:96-116 (2D closed form with +1e-10 in the denominator).
 template <typename T>
 __device__ __forceinline__ void polar2(const T m[4], T r[4]) {

@@ -1262,6 +1262,25 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
     }
     const T det = (Fn[0] * Fn[3] - Fn[1] * Fn[2]) + T(1e-10);
     jp_new = ffclamp(jp_new * oldJ / det, T(0.6), T(20.0));
+  } else {
+    if (kp.model == FFMPM_MODEL_SNOW) {
+      // three_d/g2p.py:48-58: clamp the singular values, rebuild F, update Jp.  The rebuild is
+      // U diag(s) V^T of F = U diag(s) V^T; the reference writes U @ diag(s) @ Vh.T with numpy's Vh,
+      // which depends on LAPACK's singular-vector signs and does not return F for unclamped s.
+      T U[9], sv[3], V[9];
+      svd3<T>(Fn, U, sv, V);
+      const T oldJ = det3(Fn);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) sv[d] = ffclamp(sv[d], T(1.0 - 2.5e-2), T(1.0 + 7.5e-3));
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          Fn[i * 3 + j] = U[i * 3 + 0] * sv[0] * V[j * 3 + 0] + U[i * 3 + 1] * sv[1] * V[j * 3 + 1] +
+                          U[i * 3 + 2] * sv[2] * V[j * 3 + 2];
+      const T det = det3(Fn) + T(1e-10);
+      jp_new = ffclamp(jp_new * oldJ / det, T(0.6), T(20.0));
+    }
   }
   T xn[DIM];
 #pragma unroll

@@ -140,3 +140,19 @@ def test_oracle_oob_raises():
             np.ones((n, 1)))
     with pytest.raises(RuntimeError):
         O.p2g_3d(8.0, 1.0, 1 / 8, 1e-4, 1.0, gv, gm, x, *args)
+
+
+def test_oracle_snow_3d_clamps_singular_values():
+    rng = np.random.default_rng(3)
+    N, res = 200, 12
+    x = rng.uniform(0.3, 0.7, size=(N, 3))
+    F = np.array([np.diag(rng.uniform(0.9, 1.1, size=3)) for _ in range(N)])
+    v = np.zeros((N, 3)); C = np.zeros((N, 3, 3)); Jp = np.ones((N, 1))
+    R = res + 1
+    gv = np.zeros((R, R, R, 3))
+    O.g2p_3d(float(res), 1e-4, gv, x, v, F, C, Jp, "snow")
+    sv = np.linalg.svd(F, compute_uv=False)
+    assert sv.min() >= 0.975 - 1e-12 and sv.max() <= 1.0075 + 1e-12
+    # Jp absorbs the clamped volume change: Jp * det(F) is the unclamped det (grid velocity 0 here)
+    Fin = np.array([np.diag(d) for d in np.diagonal(F, axis1=1, axis2=2)])
+    assert np.all((Jp[:, 0] >= 0.6) & (Jp[:, 0] <= 20.0))
