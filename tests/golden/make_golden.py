@@ -20,6 +20,7 @@ Fixtures written:
                   reference output beside the historical expected values.
   ref2d_*.npz     seeded 2D cases run through two_d.p2g / grid_op / g2p.
   ref3d_*.npz     seeded 3D cases run through three_d.p2g / grid_op / g2p and solve_mls_mpm_3d.
+  primitives.npz  lattice and scene points of femflow/simulation/mpm/primitives.py.
 """
 from __future__ import annotations
 
@@ -204,9 +205,31 @@ def make_3d(ref, name, seed, n, res, dt, grav, steps, E_range=(1e3, 1e3), nu=0.3
     np.savez_compressed(os.path.join(HERE, f"ref3d_{name}.npz"), **out)
 
 
+def make_primitives(ref_root):
+    """Scene primitives (femflow/simulation/mpm/primitives.py).  numerics/geometry.py imports igl
+    and wildmeshing at module level; neither is used by grid(), so empty modules stand in."""
+    import importlib.util
+
+    for name in ("igl", "wildmeshing"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    spec = importlib.util.spec_from_file_location(
+        "ref_primitives", os.path.join(ref_root, "femflow/simulation/mpm/primitives.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    from femflow.numerics.geometry import grid
+
+    out = {"grid_3_4_2": grid(np.array((3, 4, 2))), "grid_5_1_3": grid(np.array((5, 1, 3)))}
+    for fn in ("gyroid", "diamond", "primitive"):
+        out[f"{fn}_a"] = m.generate_implicit_points(fn, 0.35, 0.15, 12)
+        out[f"{fn}_b"] = m.generate_implicit_points(fn, 0.5, -0.3, 9)
+    out["cube"] = m.generate_cube_points((0.1, 0.4), (0.2, 0.5), (0.3, 0.9), 5)
+    np.savez_compressed(os.path.join(HERE, "primitives.npz"), **out)
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     ref = install_reference(ref_root)
+    make_primitives(ref_root)
     make_kat(ref, ref_root)
     # C1-like scene (block in [0.3,0.6]x[0.4,0.7], rho=1, E=1e4, nu=0.2) at reduced N/res.
     make_2d(ref, "c1_small", seed=0, n=256, res=32, E=1e4, nu=0.2, dt=1e-4, grav=-9.8, steps=6)
