@@ -78,6 +78,11 @@ _PROTOS = {
                                               _vp, ctypes.c_size_t, _vp, _P(ctypes.c_double), _P(ctypes.c_int64)]),
     "ffmpm_plan_info": (ctypes.c_int, [_P(Params), ctypes.c_int64, _P(ctypes.c_int64)]),
     "ffmpm_sort_by_block_static": (ctypes.c_int, [_P(Params), _vp, ctypes.c_int64, _vp, _vp, _vp]),
+    "ffmpm_batch2d_workspace_size": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32, _P(ctypes.c_size_t)]),
+    "ffmpm_batch2d_init": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_size_t, _vp]),
+    "ffmpm_batch2d_substeps": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _P(Particles), ctypes.c_int32,
+                                              ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_size_t, _vp]),
+    "ffmpm_batch2d_status": (ctypes.c_int, [_vp, _P(ctypes.c_int32), _vp]),
     "ffmpm_version": (ctypes.c_char_p, []),
 }
 

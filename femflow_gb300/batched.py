@@ -1,0 +1,152 @@
+"""Batched 2D scenes: many independent MLS-MPM scenes advanced by one persistent launch per substep.
+
+Each scene has its own particles, grid resolution, material (two_d.p2g's scalar ``mass``,
+``mu_0``, ``lambda_0``), dt, gravity and walls.  The particle state of all scenes lives in one set
+of component-major arrays; ``substeps`` launches one cooperative kernel per substep (P2G, grid,
+G2P of every scene with grid-wide barriers in between), ``capture`` records a CUDA graph of many
+substeps, and ``autotune`` picks the launch shape.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Dict, List
+
+import numpy as np
+import torch
+
+from . import _native as N
+from . import autotune as AT
+from . import engine as E
+
+
+class Scene2D(ctypes.Structure):
+    _fields_ = [("offset", ctypes.c_int64), ("count", ctypes.c_int64), ("res", ctypes.c_int32),
+                ("model", ctypes.c_int32), ("wall_mode", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("dx", ctypes.c_double), ("inv_dx", ctypes.c_double), ("dt", ctypes.c_double),
+                ("gravity", ctypes.c_double), ("volume", ctypes.c_double), ("hardening", ctypes.c_double),
+                ("mass", ctypes.c_double), ("mu_0", ctypes.c_double), ("lambda_0", ctypes.c_double)]
+
+
+class Batch2D:
+    """``scenes``: list of dicts with ``x`` [n,2] and scalars ``res``, ``dt``, ``mass``, ``volume``,
+    ``mu_0``, ``lambda_0`` (optional: ``v``, ``F``, ``C``, ``Jp``, ``gravity`` (-9.8),
+    ``hardening`` (1), ``model`` ("neo_hookean"), ``wall_mode`` ("reference"))."""
+
+    def __init__(self, scenes: List[Dict], dtype=torch.float32, device="cuda"):
+        E._require_cuda()
+        if not 1 <= len(scenes) <= 256:
+            raise ValueError("a batch holds 1..256 scenes")
+        self.dtype, self.device = dtype, torch.device(device)
+        self.nscenes = len(scenes)
+        counts = [int(np.asarray(s["x"]).shape[0]) for s in scenes]
+        self.offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        n = int(self.offsets[-1])
+        self.n = n
+        cat = lambda key, shape, default: np.concatenate([
+            np.asarray(s[key], dtype=np.float64).reshape(-1, *shape) if key in s and s[key] is not None else
+            default(c) for s, c in zip(scenes, counts)])
+        x = cat("x", (2,), lambda c: np.zeros((c, 2)))
+        v = cat("v", (2,), lambda c: np.zeros((c, 2)))
+        F = cat("F", (2, 2), lambda c: np.tile(np.eye(2), (c, 1, 1)))
+        C = cat("C", (2, 2), lambda c: np.zeros((c, 2, 2)))
+        Jp = np.concatenate([np.asarray(s.get("Jp", np.ones(c)), dtype=np.float64).reshape(-1)
+                             for s, c in zip(scenes, counts)])
+        dev = lambda a: torch.tensor(a, dtype=dtype, device=self.device)
+        self.x, self.v = dev(x.T.copy()), dev(v.T.copy())
+        self.F, self.C = dev(F.reshape(n, 4).T.copy()), dev(C.reshape(n, 4).T.copy())
+        self.Jp = dev(Jp)
+        table = (Scene2D * self.nscenes)()
+        for i, s in enumerate(scenes):
+            t = table[i]
+            t.offset, t.count = int(self.offsets[i]), counts[i]
+            t.res = int(s["res"])
+            t.model = N.MODELS[s.get("model", "neo_hookean")]
+            t.wall_mode = N.WALLS[s.get("wall_mode", "reference")]
+            t.dx, t.inv_dx = 1.0 / t.res, float(t.res)
+            t.dt, t.gravity = float(s["dt"]), float(s.get("gravity", -9.8))
+            t.volume, t.hardening = float(s["volume"]), float(s.get("hardening", 1.0))
+            t.mass, t.mu_0, t.lambda_0 = float(s["mass"]), float(s["mu_0"]), float(s["lambda_0"])
+        self.table = table
+        self.rb = E.real_bytes(dtype)
+        nbytes = ctypes.c_size_t(0)
+        tptr = ctypes.c_void_p(ctypes.addressof(table))
+        N.call("ffmpm_batch2d_workspace_size", tptr, self.nscenes, self.rb, ctypes.byref(nbytes))
+        self.ws_bytes = int(nbytes.value)
+        self._wsbuf = torch.empty(self.ws_bytes + 256, dtype=torch.uint8, device=self.device)
+        self.ws = (self._wsbuf.data_ptr() + 255) // 256 * 256
+        N.call("ffmpm_batch2d_init", tptr, self.nscenes, self.rb, ctypes.c_void_p(self.ws),
+               ctypes.c_size_t(self.ws_bytes), ctypes.c_void_p(E._stream_ptr(self.device)))
+        self.threads, self.ctas_per_sm = 256, 0
+        self._graph, self._graph_steps = None, 0
+
+    def _struct(self):
+        return E.particles_struct(self.x, self.v, self.F, self.C, self.Jp, stride=self.n, n=self.n)
+
+    def _launch(self, nsteps: int, threads=None, ctas=None, stream=None):
+        st = self._struct()
+        N.call("ffmpm_batch2d_substeps", self.nscenes, self.rb, ctypes.byref(st), int(nsteps),
+               int(threads or self.threads), int(self.ctas_per_sm if ctas is None else ctas),
+               ctypes.c_void_p(self.ws), ctypes.c_size_t(self.ws_bytes),
+               ctypes.c_void_p(stream if stream is not None else E._stream_ptr(self.device)))
+
+    def step(self, nsteps: int = 1):
+        if self._graph is not None and nsteps % self._graph_steps == 0:
+            for _ in range(nsteps // self._graph_steps):
+                self._graph.replay()
+        else:
+            self._launch(nsteps)
+
+    def capture(self, nsteps: int):
+        """Record `nsteps` substeps (one cooperative launch each) in a CUDA graph."""
+        self._launch(1)
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(self.device)
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self._launch(nsteps, stream=s.cuda_stream)
+        torch.cuda.synchronize(self.device)
+        self._graph, self._graph_steps = g, nsteps
+        return g
+
+    def autotune(self, steps: int = 2):
+        """Choose (threads per CTA, CTAs per SM) by timing `steps` substeps of this batch per
+        candidate.  The state advances by the substeps used for timing."""
+        sig = ("batch2d", self.nscenes, self.n, int(sum((t.res + 1) ** 2 for t in self.table)), self.rb)
+        cands = [(128, 0), (256, 0), (512, 0), (256, 2), (512, 1)]
+        best, timings = AT.tune(sig, cands, lambda c: self._launch(steps, threads=c[0], ctas=c[1]))
+        self.threads, self.ctas_per_sm = best
+        return best, timings
+
+    def status(self) -> int:
+        st = ctypes.c_int32(0)
+        N.call("ffmpm_batch2d_status", ctypes.c_void_p(self.ws), ctypes.byref(st),
+               ctypes.c_void_p(E._stream_ptr(self.device)))
+        return int(st.value)
+
+    def scene_state(self, i: int) -> Dict[str, torch.Tensor]:
+        a, b = int(self.offsets[i]), int(self.offsets[i + 1])
+        c = b - a
+        return dict(x=self.x[:, a:b].T.contiguous(), v=self.v[:, a:b].T.contiguous(),
+                    F=self.F[:, a:b].T.reshape(c, 2, 2).contiguous(),
+                    C=self.C[:, a:b].T.reshape(c, 2, 2).contiguous(), Jp=self.Jp[a:b].clone())
+
+
+def random_scenes(nscenes: int = 256, seed: int = 0, n_range=(2048, 65536), res_range=(64, 256),
+                  E_range=(1e3, 1e5), nu_range=(0.1, 0.4), dt: float = 1e-4, edge: float = 0.2) -> List[Dict]:
+    """Seeded scenes of the batched workload: particle count log-uniform in n_range, grid uniform in
+    res_range, E log-uniform in E_range, nu uniform in nu_range, a square block of particles at a
+    seeded position inside the domain margin, at rest."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nscenes):
+        n = int(round(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1])))))
+        res = int(rng.integers(res_range[0], res_range[1] + 1))
+        E = float(np.exp(rng.uniform(np.log(E_range[0]), np.log(E_range[1]))))
+        nu = float(rng.uniform(*nu_range))
+        lo = rng.uniform(0.1, 0.9 - edge, size=2)
+        x = lo + rng.uniform(0, edge, size=(n, 2))
+        vol = edge * edge / n
+        mu, lam = E / (2 * (1 + nu)), E * nu / ((1 + nu) * (1 - 2 * nu))
+        out.append(dict(x=x, res=res, dt=dt, mass=vol, volume=vol, mu_0=mu, lambda_0=lam, E=E, nu=nu))
+    return out

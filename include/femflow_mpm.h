@@ -164,6 +164,35 @@ int ffmpm_plan_info(const ffmpm_params *p, int64_t n, int64_t *info);
 int ffmpm_sort_by_block_static(const ffmpm_params *p, const void *x, int64_t n, uint32_t *keys_out,
                                uint32_t *perm_out, void *stream);
 
+/* ---- batched 2D scenes: one persistent launch per substep for many independent scenes ---- */
+#define FFMPM_BATCH2D_MAX_SCENES 256
+
+/* One scene of a batch: its particles are [offset, offset + count) of the batch's concatenated
+ * arrays (scenes in order, back to back), with the two_d.p2g scalar material and its own grid. */
+typedef struct ffmpm_scene2d {
+  int64_t offset, count;
+  int32_t res, model, wall_mode, pad;
+  double dx, inv_dx, dt, gravity, volume, hardening, mass, mu_0, lambda_0;
+} ffmpm_scene2d;
+
+/* Workspace bytes for a batch (scene table + every scene's two grids). */
+int ffmpm_batch2d_workspace_size(const ffmpm_scene2d *scenes, int32_t nscenes, int32_t real_bytes, size_t *bytes);
+
+/* Copy the scene table into the workspace and zero the grids (synchronises `stream`). */
+int ffmpm_batch2d_init(const ffmpm_scene2d *scenes, int32_t nscenes, int32_t real_bytes, void *ws, size_t ws_bytes,
+                       void *stream);
+
+/* `nsteps` substeps of every scene: per substep one cooperative launch that runs P2G, the grid
+ * update and G2P of all scenes, separated by grid-wide barriers (two_d/p2g.py, grid_op.py, g2p.py
+ * per scene).  `threads` (128/256/512) and `ctas_per_sm` (0 = as many as fit) set the launch
+ * shape; the autotuner chooses them.  Particles are updated in place.  No reference counterpart
+ * (the reference steps one scene at a time). */
+int ffmpm_batch2d_substeps(int32_t nscenes, int32_t real_bytes, ffmpm_particles *P, int32_t nsteps, int32_t threads,
+                           int32_t ctas_per_sm, void *ws, size_t ws_bytes, void *stream);
+
+/* Status word of a batch workspace (FFMPM_STATUS_* bits); synchronises `stream`. */
+int ffmpm_batch2d_status(void *ws, int32_t *status, void *stream);
+
 /* Library version string. */
 const char *ffmpm_version(void);
 

@@ -1,0 +1,78 @@
+"""Batched 2D scenes (one persistent launch per substep) against the oracle and the single-scene path."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from gpu_helpers import TOL, close, n, sign_align, t
+from femflow_gb300.batched import Batch2D, random_scenes
+from femflow_gb300.solvers.mpm import two_d
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(seed=1):
+    sc = random_scenes(7, seed=seed, n_range=(300, 3000), res_range=(24, 96), E_range=(5e2, 5e3))
+    sc[3]["model"] = "snow"
+    sc[3]["hardening"] = 10.0
+    sc[5]["wall_mode"] = "sticky3"
+    for s in sc:  # some motion so C and F evolve
+        rng = np.random.default_rng(len(s["x"]))
+        s["v"] = rng.normal(0, 0.3, size=(len(s["x"]), 2))
+    return sc
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_batch_matches_oracle_per_scene(dtype):
+    sc = small_batch()
+    b = Batch2D(sc, dtype=dtype)
+    steps = 5
+    b.step(steps)
+    assert b.status() == 0
+    tol = TOL[dtype]
+    for i, s in enumerate(sc):
+        if s.get("wall_mode", "reference") != "reference":
+            continue  # the oracle implements the reference walls only
+        x = s["x"].copy(); v = s["v"].copy(); N_ = len(x)
+        F = np.tile(np.eye(2), (N_, 1, 1)); C = np.zeros((N_, 2, 2)); Jp = np.ones((N_, 1))
+        for _ in range(steps):
+            O.substep_2d(s["res"], float(s["res"]), s.get("hardening", 1.0), s["mu_0"], s["lambda_0"], s["mass"],
+                         1.0 / s["res"], s["dt"], s["volume"], -9.8, x, v, F, C, Jp, s.get("model", "neo_hookean"))
+        st = b.scene_state(i)
+        close(n(st["x"]), x, 5 * tol["x"], scale=1.0, what=f"scene {i} x")
+        close(n(st["v"]), v, 5 * tol["v"], scale=np.abs(v).max(), what=f"scene {i} v")
+        close(sign_align(n(st["F"]), F), F, 10 * tol["F"], scale=1.0, what=f"scene {i} F")
+
+
+def test_batch_matches_single_scene_path_with_sticky_walls():
+    sc = small_batch(seed=2)
+    b = Batch2D(sc, dtype=torch.float64)
+    b.step(4)
+    for i in (5,):
+        s = sc[i]
+        dtype = torch.float64
+        x, v = t(s["x"], dtype), t(s["v"], dtype)
+        N_ = x.shape[0]
+        F = torch.eye(2, dtype=dtype, device="cuda").repeat(N_, 1, 1).contiguous()
+        C = torch.zeros((N_, 2, 2), dtype=dtype, device="cuda")
+        Jp = torch.ones((N_, 1), dtype=dtype, device="cuda")
+        for _ in range(4):
+            two_d.solve_mls_mpm_2d(s["res"], float(s["res"]), 1.0, s["mu_0"], s["lambda_0"], s["mass"], 1.0 / s["res"],
+                                   s["dt"], s["volume"], -9.8, x, v, F, C, Jp, wall_mode="sticky3")
+        st = b.scene_state(i)
+        close(n(st["x"]), n(x), 1e-12, scale=1.0, what="x sticky3")
+
+
+def test_batch_graph_replay_and_autotune():
+    sc = small_batch(seed=3)
+    a = Batch2D(sc, dtype=torch.float64)
+    c = Batch2D(sc, dtype=torch.float64)
+    best, timings = a.autotune(steps=1)  # advances a by 1 substep per candidate tried
+    assert best in [(128, 0), (256, 0), (512, 0), (256, 2), (512, 1)]
+    used = len(timings) * 2 if timings else 0  # time_call: 1 warm-up + 3 timed launches of `steps`
+    a2 = Batch2D(sc, dtype=torch.float64)
+    a2.capture(4)  # one direct substep before capturing
+    a2.step(8)
+    c.step(9)
+    close(n(a2.scene_state(2)["x"]), n(c.scene_state(2)["x"]), 1e-12, scale=1.0, what="graph vs direct")
+    assert a.status() == 0 and a2.status() == 0
