@@ -29,7 +29,7 @@ STATUS_OOB = 1
 STATUS_NONFINITE = 2
 STATUS_TIMEOUT = 4
 
-MODELS = {"neo_hookean": 0, "snow": 1}
+MODELS = {"neo_hookean": 0, "snow": 1, "fixed_corotated": 2}
 NPHASES = 6
 PHASES = ("keys", "sort", "plan", "p2g", "grid_update", "g2p")
 WALLS = {"reference": 0, "sticky3": 1}
@@ -54,6 +54,11 @@ class Particles(ctypes.Structure):
 
 class Grid(ctypes.Structure):
     _fields_ = [("velocity", ctypes.c_void_p), ("mass", ctypes.c_void_p)]
+
+
+class Adjoint(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_void_p), ("v", ctypes.c_void_p), ("F", ctypes.c_void_p), ("C", ctypes.c_void_p),
+                ("mu_0", ctypes.c_void_p), ("lambda_0", ctypes.c_void_p)]
 
 
 _lib = None
@@ -83,6 +88,8 @@ _PROTOS = {
     "ffmpm_batch2d_substeps": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _P(Particles), ctypes.c_int32,
                                               ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_size_t, _vp]),
     "ffmpm_batch2d_status": (ctypes.c_int, [_vp, _P(ctypes.c_int32), _vp]),
+    "ffmpm_adjoint_workspace_size": (ctypes.c_int, [_P(Params), ctypes.c_int64, _P(ctypes.c_size_t)]),
+    "ffmpm_substep_adjoint": (ctypes.c_int, [_P(Params), _P(Particles), _P(Adjoint), _vp, ctypes.c_size_t, _vp]),
     "ffmpm_version": (ctypes.c_char_p, []),
 }
 

@@ -244,7 +244,9 @@ __global__ void __launch_bounds__(kBatchMaxThreads) k_batch2d_substep(unsigned c
     if (!ok) continue;
     const int R = kp.res + 1;
     const Node4<T>* grid = B + s_noff[si];
+    // node velocities relative to the stencil's centre node (the bulk velocity cancels exactly in C)
     T v[2] = {T(0), T(0)}, Cn[4] = {T(0), T(0), T(0), T(0)};
+    const Node4<T> uc = grid[(int64_t)(b[0] + 1) * R + (b[1] + 1)];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       const T d0 = T(i) - fx[0];
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads) k_batch2d_substep(unsigned c
         const T d1 = T(j) - fx[1];
         const T wt = w[i][0] * w[j][1];
         const Node4<T> gv = grid[(int64_t)(b[0] + i) * R + (b[1] + j)];
-        const T wv0 = wt * gv.x, wv1 = wt * gv.y;
+        const T wv0 = wt * (gv.x - uc.x), wv1 = wt * (gv.y - uc.y);
         v[0] += wv0;
         v[1] += wv1;
         Cn[0] += wv0 * d0;
@@ -262,6 +264,8 @@ __global__ void __launch_bounds__(kBatchMaxThreads) k_batch2d_substep(unsigned c
         Cn[3] += wv1 * d1;
       }
     }
+    v[0] += uc.x;
+    v[1] += uc.y;
     const T c4 = T(4) * kp.inv_dx;
 #pragma unroll
     for (int i = 0; i < 4; ++i) Cn[i] *= c4;
@@ -269,10 +273,11 @@ __global__ void __launch_bounds__(kBatchMaxThreads) k_batch2d_substep(unsigned c
 #pragma unroll
     for (int i = 0; i < 4; ++i) F[i] = P.F[P.at(p, i, 4)];
     T Fn[4];
-    Fn[0] = (T(1) + kp.dt * Cn[0]) * F[0] + kp.dt * Cn[1] * F[2];
-    Fn[1] = (T(1) + kp.dt * Cn[0]) * F[1] + kp.dt * Cn[1] * F[3];
-    Fn[2] = kp.dt * Cn[2] * F[0] + (T(1) + kp.dt * Cn[3]) * F[2];
-    Fn[3] = kp.dt * Cn[2] * F[1] + (T(1) + kp.dt * Cn[3]) * F[3];
+    // F + dt (C F): (I + dt C) F with the increment rounded once against F
+    Fn[0] = F[0] + kp.dt * (Cn[0] * F[0] + Cn[1] * F[2]);
+    Fn[1] = F[1] + kp.dt * (Cn[0] * F[1] + Cn[1] * F[3]);
+    Fn[2] = F[2] + kp.dt * (Cn[2] * F[0] + Cn[3] * F[2]);
+    Fn[3] = F[3] + kp.dt * (Cn[2] * F[1] + Cn[3] * F[3]);
     const T oldJ = Fn[0] * Fn[3] - Fn[1] * Fn[2];
     if (kp.model == FFMPM_MODEL_SNOW) {
       T U[4], s2[2], V[4];

@@ -37,7 +37,8 @@ bool valid_params(const ffmpm_params* p) {
   if (p->dim != 2 && p->dim != 3) return false;
   if (p->real_bytes != 4 && p->real_bytes != 8) return false;
   if (p->res < 3 || p->res > 4096) return false;
-  if (p->model != FFMPM_MODEL_NEO_HOOKEAN && p->model != FFMPM_MODEL_SNOW) return false;
+  if (p->model != FFMPM_MODEL_NEO_HOOKEAN && p->model != FFMPM_MODEL_SNOW && p->model != FFMPM_MODEL_FIXED_COROTATED)
+    return false;
   if (p->wall_mode != FFMPM_WALLS_REFERENCE && p->wall_mode != FFMPM_WALLS_STICKY3) return false;
   if (p->block_size != 0 && (p->block_size < 2 || p->block_size > 16 || (p->block_size & (p->block_size - 1))))
     return false;
@@ -135,41 +136,6 @@ bool encode_grid_map(CUtensorMap* map, void* base, const Layout& L) {
   CUresult r = fn(map, dt, rank, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
-}
-
-template <typename T>
-KParams<T> kparams(const ffmpm_params& p) {
-  KParams<T> k;
-  k.dx = T(p.dx);
-  k.inv_dx = T(p.inv_dx);
-  k.dt = T(p.dt);
-  k.gravity = T(p.gravity);
-  k.volume = T(p.volume);
-  k.hardening = T(p.hardening);
-  k.mass = T(p.mass);
-  k.mu0 = T(p.mu_0);
-  k.lam0 = T(p.lambda_0);
-  k.v_allowed = T(p.dx * 0.9 / p.dt);  // three_d/grid_op.py:25, computed in double as the reference
-  k.res = p.res;
-  k.model = p.model;
-  k.wall_mode = p.wall_mode;
-  k.variant = p.variant;
-  return k;
-}
-
-template <typename T>
-PView<T> pview(const ffmpm_particles& P) {
-  PView<T> v;
-  v.x = static_cast<T*>(P.x);
-  v.v = static_cast<T*>(P.v);
-  v.F = static_cast<T*>(P.F);
-  v.C = static_cast<T*>(P.C);
-  v.Jp = static_cast<T*>(P.Jp);
-  v.mass = static_cast<T*>(const_cast<void*>(P.mass));
-  v.mu0 = static_cast<T*>(const_cast<void*>(P.mu_0));
-  v.lam0 = static_cast<T*>(const_cast<void*>(P.lambda_0));
-  v.soa = P.stride;
-  return v;
 }
 
 template <int DIM>

@@ -41,6 +41,43 @@ struct PView {
   }
 };
 
+// Kernel parameters and particle view of the C-ABI structs (host side).
+template <typename T>
+inline KParams<T> kparams(const ffmpm_params& p) {
+  KParams<T> k;
+  k.dx = T(p.dx);
+  k.inv_dx = T(p.inv_dx);
+  k.dt = T(p.dt);
+  k.gravity = T(p.gravity);
+  k.volume = T(p.volume);
+  k.hardening = T(p.hardening);
+  k.mass = T(p.mass);
+  k.mu0 = T(p.mu_0);
+  k.lam0 = T(p.lambda_0);
+  k.v_allowed = T(p.dx * 0.9 / p.dt);  // three_d/grid_op.py:25, computed in double as the reference
+  k.res = p.res;
+  k.model = p.model;
+  k.wall_mode = p.wall_mode;
+  k.variant = p.variant;
+  return k;
+}
+
+template <typename T>
+inline PView<T> pview(const ffmpm_particles& P) {
+  PView<T> v;
+  v.x = static_cast<T*>(P.x);
+  v.v = static_cast<T*>(P.v);
+  v.F = static_cast<T*>(P.F);
+  v.C = static_cast<T*>(P.C);
+  v.Jp = static_cast<T*>(P.Jp);
+  v.mass = static_cast<T*>(const_cast<void*>(P.mass));
+  v.mu0 = static_cast<T*>(const_cast<void*>(P.mu_0));
+  v.lam0 = static_cast<T*>(const_cast<void*>(P.lambda_0));
+  v.soa = P.stride;
+  return v;
+}
+
+
 template <int DIM>
 __device__ __forceinline__ void block_coords(const Geom<DIM>& g, int blk, int c[DIM]) {
   if constexpr (DIM == 3) {
@@ -234,25 +271,91 @@ __device__ __forceinline__ int tile_nodes(const Geom<DIM>& g) {
 }
 
 // Stress + APIC affine matrix of one particle (utils.py:95-135 / 52-92):
-//   A = -(dt*vol) * (4*inv_dx^2 * PF) + m*C,  PF = 2mu(F-R)F^T + lam(J-1)J  (scalar on all entries)
+//   A = -(dt*vol) * (4*inv_dx^2 * PF) + m*C,  PF = 2mu(F-R)F^T + lam(J-1)J  (scalar on all entries;
+//   on the diagonal only for FFMPM_MODEL_FIXED_COROTATED)
+// F - R for F close to a rotation, without forming R: with S = sqrt(F^T F) = I + Y,
+// F - R = F (I - S^-1) = F Y (I + Y)^-1, and Y = S - I is the fixed point of Y = (E - Y^2) / 2 with
+// E = F^T F - I = H + H^T + H^T H, H = F - I.  Every quantity is of the size of the strain, so F - R
+// keeps float's relative precision; Newton's R has an absolute error of ~1e-7, which at strain 1e-4
+// leaves F - R with three correct digits.  Applies when max |E| <= 0.05 (then |Y| < 0.1 and eight
+// iterations reach float precision); returns false otherwise.
+template <typename T>
+__device__ __forceinline__ bool f_minus_r_small_strain3(const T F[9], T FmR[9]) {
+  T H[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) H[i] = F[i] - (i % 4 == 0 ? T(1) : T(0));
+  T E[9], emax = T(0);
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      const T e = H[a * 3 + b] + H[b * 3 + a] + H[0 * 3 + a] * H[0 * 3 + b] + H[1 * 3 + a] * H[1 * 3 + b] +
+                  H[2 * 3 + a] * H[2 * 3 + b];
+      E[a * 3 + b] = e;
+      emax = ffabs(e) > emax ? ffabs(e) : emax;
+    }
+  if (!(emax <= T(0.05))) return false;
+  T Y[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Y[i] = T(0.5) * E[i];
+#pragma unroll
+  for (int it = 0; it < 8; ++it) {
+    T Yn[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+        Yn[a * 3 + b] = T(0.5) * (E[a * 3 + b] - (Y[a * 3 + 0] * Y[0 * 3 + b] + Y[a * 3 + 1] * Y[1 * 3 + b] +
+                                                  Y[a * 3 + 2] * Y[2 * 3 + b]));
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Y[i] = Yn[i];
+  }
+  T M[9], Mc[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) M[i] = Y[i] + (i % 4 == 0 ? T(1) : T(0));
+  cofactor3(M, Mc);
+  const T inv_det = T(1) / (M[0] * Mc[0] + M[1] * Mc[1] + M[2] * Mc[2]);
+  T FY[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+      FY[a * 3 + b] = F[a * 3 + 0] * Y[0 * 3 + b] + F[a * 3 + 1] * Y[1 * 3 + b] + F[a * 3 + 2] * Y[2 * 3 + b];
+  // (I + Y)^-1 = cof(I + Y)^T / det, and cof of a symmetric matrix is symmetric
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+      FmR[a * 3 + b] = (FY[a * 3 + 0] * Mc[0 * 3 + b] + FY[a * 3 + 1] * Mc[1 * 3 + b] + FY[a * 3 + 2] * Mc[2 * 3 + b]) *
+                       inv_det;
+  return true;
+}
+
 template <int DIM, typename T>
 __device__ __forceinline__ void affine_of(const KParams<T>& kp, const T* F, const T* C, T m, T mu, T lam, T* A,
                                           uint32_t* fallbacks) {
   const T Dinv = T(4) * kp.inv_dx * kp.inv_dx;
   const T s = -(kp.dt * kp.volume);
   if constexpr (DIM == 3) {
-    T R[9];
-    polar3<T>(F, R, fallbacks);
+    T FmR[9];
+    bool small = false;
+    if constexpr (sizeof(T) == 4) small = f_minus_r_small_strain3(F, FmR);
+    if (!small) {
+      T R[9];
+      polar3<T>(F, R, fallbacks);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) FmR[i] = F[i] - R[i];
+    }
     const T J = det3(F);
     const T sc = lam * (J - T(1)) * J;
-    T FmR[9];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) FmR[i] = T(2) * mu * (F[i] - R[i]);
+    for (int i = 0; i < 9; ++i) FmR[i] *= T(2) * mu;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        const T pf = FmR[i * 3 + 0] * F[j * 3 + 0] + FmR[i * 3 + 1] * F[j * 3 + 1] + FmR[i * 3 + 2] * F[j * 3 + 2] + sc;
+        const T pf = FmR[i * 3 + 0] * F[j * 3 + 0] + FmR[i * 3 + 1] * F[j * 3 + 1] + FmR[i * 3 + 2] * F[j * 3 + 2] +
+                     ((i == j || kp.model != FFMPM_MODEL_FIXED_COROTATED) ? sc : T(0));
         A[i * 3 + j] = s * (Dinv * pf) + m * C[i * 3 + j];
       }
   } else {
@@ -267,7 +370,8 @@ __device__ __forceinline__ void affine_of(const KParams<T>& kp, const T* F, cons
     for (int i = 0; i < 2; ++i)
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
-        const T pf = FmR[i * 2 + 0] * F[j * 2 + 0] + FmR[i * 2 + 1] * F[j * 2 + 1] + sc;
+        const T pf = FmR[i * 2 + 0] * F[j * 2 + 0] + FmR[i * 2 + 1] * F[j * 2 + 1] +
+                     ((i == j || kp.model != FFMPM_MODEL_FIXED_COROTATED) ? sc : T(0));
         A[i * 2 + j] = s * (Dinv * pf) + m * C[i * 2 + j];
       }
   }
@@ -1182,13 +1286,23 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
     raise_status(status, FFMPM_STATUS_OOB);
     return;
   }
+  // The gather runs on node velocities relative to the stencil's centre node u: v = u + sum w (v_i - u)
+  // and C = 4 inv_dx sum w (v_i - u) (x) (i - fx), equal in exact arithmetic to the reference's
+  // sums (the weights sum to 1 and sum w (i - fx) = 0).  A body's bulk velocity then cancels exactly
+  // instead of leaving rounding residue of size |u| eps inv_dx in C, which in float would drift F
+  // by ~1e-5 over a thousand substeps of a falling or colliding body.
   T v[DIM], Cn[DD];
 #pragma unroll
   for (int d = 0; d < DIM; ++d) v[d] = T(0);
 #pragma unroll
   for (int i = 0; i < DD; ++i) Cn[i] = T(0);
   const int T1 = g.tile;
+  T u[DIM];
   if constexpr (DIM == 3) {
+    const Node4<T> c = tile[((lb[0] + 1) * T1 + (lb[1] + 1)) * T1 + (lb[2] + 1)];
+    u[0] = c.x;
+    u[1] = c.y;
+    u[2] = c.z;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       const T d0 = T(i) - fx[0];
@@ -1201,7 +1315,7 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
           const T d2 = T(k) - fx[2];
           const T weight = wij * w[k][2];
           const Node4<T> gvn = tile[((lb[0] + i) * T1 + (lb[1] + j)) * T1 + (lb[2] + k)];
-          const T wv0 = weight * gvn.x, wv1 = weight * gvn.y, wv2 = weight * gvn.z;
+          const T wv0 = weight * (gvn.x - u[0]), wv1 = weight * (gvn.y - u[1]), wv2 = weight * (gvn.z - u[2]);
           v[0] += wv0;
           v[1] += wv1;
           v[2] += wv2;
@@ -1212,6 +1326,9 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
       }
     }
   } else {
+    const Node4<T> c = tile[(lb[0] + 1) * T1 + (lb[1] + 1)];
+    u[0] = c.x;
+    u[1] = c.y;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       const T d0 = T(i) - fx[0];
@@ -1220,7 +1337,7 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
         const T d1 = T(j) - fx[1];
         const T weight = w[i][0] * w[j][1];
         const Node4<T> gvn = tile[(lb[0] + i) * T1 + (lb[1] + j)];
-        const T wv0 = weight * gvn.x, wv1 = weight * gvn.y;
+        const T wv0 = weight * (gvn.x - u[0]), wv1 = weight * (gvn.y - u[1]);
         v[0] += wv0;
         v[1] += wv1;
         Cn[0] += wv0 * d0; Cn[1] += wv0 * d1;
@@ -1228,21 +1345,25 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
       }
     }
   }
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) v[d] += u[d];
   const T c4 = T(4) * kp.inv_dx;
 #pragma unroll
   for (int i = 0; i < DD; ++i) Cn[i] *= c4;
   T F[DD], Fn[DD];
 #pragma unroll
   for (int i = 0; i < DD; ++i) F[i] = in.F[i];
-  // F <- (I + dt C) F   (g2p.py:46)
+  // F <- (I + dt C) F   (g2p.py:46), evaluated as F + dt (C F): the increment is formed on its own
+  // and rounded once against F, where 1 + dt C would round dt C to the spacing of the numbers near
+  // 1 (in float that keeps only ~3 digits of a 1e-4 increment)
 #pragma unroll
   for (int r = 0; r < DIM; ++r)
 #pragma unroll
     for (int c = 0; c < DIM; ++c) {
       T acc = T(0);
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) acc += ((r == k ? T(1) : T(0)) + kp.dt * Cn[r * DIM + k]) * F[k * DIM + c];
-      Fn[r * DIM + c] = acc;
+      for (int k = 0; k < DIM; ++k) acc += Cn[r * DIM + k] * F[k * DIM + c];
+      Fn[r * DIM + c] = F[r * DIM + c] + kp.dt * acc;
     }
   const bool write_jp = (DIM == 2) || sorted || kp.model == FFMPM_MODEL_SNOW;
   T jp_new = in.jp;

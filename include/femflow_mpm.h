@@ -47,6 +47,11 @@ extern "C" {
 /* material models: reference strings of three_d/p2g.py:57-61 */
 #define FFMPM_MODEL_NEO_HOOKEAN 0 /* "neo_hookean": fixed-corotated stress, constant hardening */
 #define FFMPM_MODEL_SNOW 1        /* "snow": exp hardening in P2G + singular-value clamp in G2P */
+/* "fixed_corotated": the textbook fixed-corotated stress PF = 2mu(F-R)F^T + lam(J-1)J I (the volume term
+ * on the diagonal only), constant hardening.  Not a reference model: the reference's "neo_hookean"
+ * adds lam(J-1)J to all nine entries of PF (utils.py:129), a stress that derives from no energy and
+ * makes long elastic runs grow. */
+#define FFMPM_MODEL_FIXED_COROTATED 2
 
 /* boundary rules of the grid update */
 #define FFMPM_WALLS_REFERENCE 0 /* 3D: three_d/grid_op.py:38-47;  2D: two_d/grid_op.py:13-24 */
@@ -192,6 +197,33 @@ int ffmpm_batch2d_substeps(int32_t nscenes, int32_t real_bytes, ffmpm_particles 
 
 /* Status word of a batch workspace (FFMPM_STATUS_* bits); synchronises `stream`. */
 int ffmpm_batch2d_status(void *ws, int32_t *status, void *stream);
+
+/* ---- adjoint of one 3D substep (reverse mode, for differentiable rollouts) ---- */
+
+/* Adjoints of a particle state, laid out exactly like the ffmpm_particles they belong to (same
+ * real type, same `stride`).  On entry x, v, F, C hold dL/d(state after the substep); on return
+ * they hold dL/d(state before it).  mu_0 / lambda_0 (nullable, always double, one per particle)
+ * are ADDED TO: dL/dmu_0 and dL/dlambda_0 of this substep's stress, per particle (sum them for a
+ * uniform material). */
+typedef struct ffmpm_adjoint {
+  void *x, *v, *F, *C;
+  double *mu_0, *lambda_0;
+} ffmpm_adjoint;
+
+/* Workspace bytes of ffmpm_substep_adjoint (status header + two dense (res+1)^3 grids of float64
+ * nodes, 32 bytes each, for either real type). */
+int ffmpm_adjoint_workspace_size(const ffmpm_params *p, int64_t n, size_t *bytes);
+
+/* Reverse of one ffmpm_substep (3D, model FFMPM_MODEL_NEO_HOOKEAN or FFMPM_MODEL_FIXED_COROTATED, either
+ * wall mode) at the state
+ * P (the state BEFORE the substep; P is only read).  The substep's grid is recomputed from P, then
+ * G2P is reversed as a scatter of node-velocity adjoints, the grid update as a per-node rule (the
+ * division by mass, the clamp and the walls pass no gradient where they clip), and P2G as a gather
+ * that also differentiates the stress, including the polar factor.  The workspace's status header
+ * reads with ffmpm_status_read.  Other dims/models: FFMPM_ERR_UNSUPPORTED.  The reference has no
+ * derivative; this is the exact derivative of solve_mls_mpm_3d (mls_mpm.py:40-79). */
+int ffmpm_substep_adjoint(const ffmpm_params *p, const ffmpm_particles *P, ffmpm_adjoint *A, void *ws,
+                          size_t ws_bytes, void *stream);
 
 /* Library version string. */
 const char *ffmpm_version(void);

@@ -25,7 +25,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "liboracle_mpm.so")
 _lib = None
 
-MODELS = {"neo_hookean": 0, "snow": 1}
+MODELS = {"neo_hookean": 0, "snow": 1, "fixed_corotated": 2}
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _d = ctypes.c_double

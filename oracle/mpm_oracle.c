@@ -40,6 +40,7 @@
 
 #define MODEL_NEO_HOOKEAN 0 /* reference string "neo_hookean": fixed-corotated + constant hardening */
 #define MODEL_SNOW 1
+#define MODEL_FIXED_COROTATED 2 /* textbook stress: lam(J-1)J on the diagonal of PF only (not a reference model) */
 
 /* ------------------------------------------------------------------ small 3x3 helpers */
 
@@ -187,7 +188,7 @@ static void hardening_lame(int model, double mu0, double lam0, double h, double 
 
 /* utils.py:95-135: A = -(dt*vol)*(4*inv_dx^2*PF) + m*C,  PF = 2mu(F-R)F^T + lam(J-1)J (scalar on all 9). */
 static void stress_affine_3d(const double *F, double inv_dx, double mu, double lam, double dt, double vol,
-                             double mass, const double *C, double *A) {
+                             double mass, const double *C, double *A, int model) {
     double J = det3(F);
     double R[9];
     polar3(F, R);
@@ -199,14 +200,14 @@ static void stress_affine_3d(const double *F, double inv_dx, double mu, double l
     mm3(FmR, Ft, PF);
     double sc = lam * (J - 1.0) * J;
     for (int i = 0; i < 9; ++i) {
-        PF[i] += sc;
+        if (model != MODEL_FIXED_COROTATED || i % 4 == 0) PF[i] += sc;
         A[i] = -(dt * vol) * (Dinv * PF[i]) + mass * C[i];
     }
 }
 
 /* utils.py:52-92 (2D). */
 static void stress_affine_2d(const double *F, double inv_dx, double mu, double lam, double dt, double vol,
-                             double mass, const double *C, double *A) {
+                             double mass, const double *C, double *A, int model) {
     double J = det2(F);
     double R[4];
     polar2(F, R);
@@ -219,7 +220,8 @@ static void stress_affine_2d(const double *F, double inv_dx, double mu, double l
     PF[2] = FmR[2] * F[0] + FmR[3] * F[1];
     PF[3] = FmR[2] * F[2] + FmR[3] * F[3];
     double sc = lam * (J - 1.0) * J;
-    for (int i = 0; i < 4; ++i) A[i] = -(dt * vol) * (Dinv * (PF[i] + sc)) + mass * C[i];
+    for (int i = 0; i < 4; ++i)
+        A[i] = -(dt * vol) * (Dinv * (PF[i] + ((model != MODEL_FIXED_COROTATED || i % 3 == 0) ? sc : 0.0))) + mass * C[i];
 }
 
 /* quadratic B-spline weights, p2g.py:55 */
@@ -258,7 +260,7 @@ int orc_p2g_3d(double inv_dx, double hardening, double dx, double dt, double vol
         }
         double mu, lam, A[9];
         hardening_lame(model, mu0[p], lam0[p], hardening, Jp[p], &mu, &lam);
-        stress_affine_3d(&F[p * 9], inv_dx, mu, lam, dt, volume, mass[p], &C[p * 9], A);
+        stress_affine_3d(&F[p * 9], inv_dx, mu, lam, dt, volume, mass[p], &C[p * 9], A, model);
         double m = mass[p];
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j)
@@ -384,7 +386,7 @@ int orc_p2g_2d(double inv_dx, double hardening, double mu_0, double lambda_0, do
         }
         double mu, lam, A[4];
         hardening_lame(model, mu_0, lambda_0, hardening, Jp[p], &mu, &lam);
-        stress_affine_2d(&F[p * 4], inv_dx, mu, lam, dt, volume, mass, &C[p * 4], A);
+        stress_affine_2d(&F[p * 4], inv_dx, mu, lam, dt, volume, mass, &C[p * 4], A, model);
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) {
                 double dpos[2] = {((double)i - fx[0]) * dx, ((double)j - fx[1]) * dx};
@@ -493,11 +495,11 @@ void orc_polar_2d(const double *F, double *R) { polar2(F, R); }
 void orc_svd_3d(const double *F, double *U, double *s, double *V) { svd3(F, U, s, V); }
 void orc_stress_affine_3d(const double *F, double inv_dx, double mu, double lam, double dt, double vol,
                           double mass, const double *C, double *A) {
-    stress_affine_3d(F, inv_dx, mu, lam, dt, vol, mass, C, A);
+    stress_affine_3d(F, inv_dx, mu, lam, dt, vol, mass, C, A, 0);
 }
 void orc_stress_affine_2d(const double *F, double inv_dx, double mu, double lam, double dt, double vol,
                           double mass, const double *C, double *A) {
-    stress_affine_2d(F, inv_dx, mu, lam, dt, vol, mass, C, A);
+    stress_affine_2d(F, inv_dx, mu, lam, dt, vol, mass, C, A, 0);
 }
 
 /* ------------------------------------------------------------------ multi-threaded timing variant
@@ -540,7 +542,7 @@ int orc_substep_3d_par(int res, double inv_dx, double hardening, double dx, doub
         }
         double mu, lam, A[9];
         hardening_lame(model, mu0[p], lam0[p], hardening, Jp[p], &mu, &lam);
-        stress_affine_3d(&F[p * 9], inv_dx, mu, lam, dt, volume, mass[p], &C[p * 9], A);
+        stress_affine_3d(&F[p * 9], inv_dx, mu, lam, dt, volume, mass[p], &C[p * 9], A, model);
         double m = mass[p];
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j)

@@ -105,3 +105,25 @@ def test_c1_scene_against_oracle(dtype):
     close(n(gx), x, 10 * tol["x"], scale=1.0, what="x")
     close(n(gvv), v, 10 * tol["v"], scale=np.abs(v).max(), what="v")
     close(sign_align(n(gF), F), F, 10 * tol["F"], scale=1.0, what="F")
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_fixed_corotated_model_against_oracle(dtype):
+    """The textbook fixed-corotated stress (not a reference model), 2D phases vs the FP64 C oracle."""
+    rng = np.random.default_rng(8)
+    N, res, dt, g, vol, mass, mu, lam = 4000, 64, 1e-4, -9.8, 1e-5, 1e-5, 400.0, 600.0
+    x = rng.uniform(0.2, 0.8, (N, 2)); v = rng.normal(0, 0.3, (N, 2))
+    F = np.eye(2)[None] + rng.normal(0, 0.05, (N, 2, 2)); C = rng.normal(0, 1.0, (N, 2, 2)); Jp = np.ones((N, 1))
+    gv = np.zeros((res + 1, res + 1, 2)); gm = np.zeros((res + 1, res + 1, 1))
+    dx_, dv, dF, dC, dJ, dgv, dgm = (t(a, dtype) for a in (x, v, F, C, Jp, gv, gm))
+    O.p2g_2d(float(res), 1.0, mu, lam, mass, 1 / res, dt, vol, gv, gm, x, v, F, C, Jp, model="fixed_corotated")
+    two_d.p2g(float(res), 1.0, mu, lam, mass, 1 / res, dt, vol, dgv, dgm, dx_, dv, dF, dC, dJ, "fixed_corotated")
+    tol = TOL[dtype]
+    close(n(dgv), gv, tol["grid"], scale=np.abs(gv).max(), what="momentum")
+    O.grid_op_2d(res, dt, g, gv, gm)
+    two_d.grid_op(res, dt, g, dgv, dgm)
+    O.g2p_2d(float(res), dt, gv, x, v, F, C, Jp, model="fixed_corotated")
+    two_d.g2p(float(res), dt, dgv, dx_, dv, dF, dC, dJ, "fixed_corotated")
+    close(n(dx_), x, tol["x"], scale=1.0, what="x")
+    close(n(dv), v, tol["v"], scale=np.abs(v).max(), what="v")
+    close(sign_align(n(dF), F), F, tol["F"], scale=1.0, what="F")
