@@ -90,6 +90,8 @@ _PROTOS = {
     "ffmpm_batch2d_status": (ctypes.c_int, [_vp, _P(ctypes.c_int32), _vp]),
     "ffmpm_adjoint_workspace_size": (ctypes.c_int, [_P(Params), ctypes.c_int64, _P(ctypes.c_size_t)]),
     "ffmpm_substep_adjoint": (ctypes.c_int, [_P(Params), _P(Particles), _P(Adjoint), _vp, ctypes.c_size_t, _vp]),
+    "ffmpm_tc_gemm_bf16": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.c_int32, _vp, _vp]),
     "ffmpm_version": (ctypes.c_char_p, []),
 }
 

@@ -225,6 +225,16 @@ int ffmpm_adjoint_workspace_size(const ffmpm_params *p, int64_t n, size_t *bytes
 int ffmpm_substep_adjoint(const ffmpm_params *p, const ffmpm_particles *P, ffmpm_adjoint *A, void *ws,
                           size_t ws_bytes, void *stream);
 
+/* ---- BF16 tensor-core (tcgen05) kernels of the learned corrector ---- */
+
+/* D[M][N] (float32, row-major) = A[M][K] . B[N][K]^T, with A and B bf16 row-major (raw 16-bit
+ * words) and float32 accumulation in tensor memory.  M % 128 == 0, N % 16 == 0 and N <= 256,
+ * K % 64 == 0, A and B 16-byte aligned.  split_k > 1 splits K over up to that many CTAs, which then
+ * ADD into D (zero D first); split_k = 1 overwrites D.  `status` (device int32, nullable) gets
+ * FFMPM_STATUS_TIMEOUT if a bounded wait on the tensor core expired.  No reference counterpart. */
+int ffmpm_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, float *D, int32_t M, int32_t N, int32_t K,
+                       int32_t split_k, int32_t *status, void *stream);
+
 /* Library version string. */
 const char *ffmpm_version(void);
 
