@@ -61,6 +61,21 @@ class Adjoint(ctypes.Structure):
                 ("mu_0", ctypes.c_void_p), ("lambda_0", ctypes.c_void_p)]
 
 
+MLP_IN, MLP_FEATURES, MLP_HIDDEN, MLP_OUT, MLP_PARAMS = 128, 113, 64, 12, 41168
+MLP_OFF = {"W1": 0, "W2": 16384, "W3": 24576, "W4": 32768, "b1": 40960, "b2": 41024, "b3": 41088, "b4": 41152}
+
+
+class MLP(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in ("W1", "W2", "W3", "W4", "b1", "b2", "b3", "b4", "in_scale",
+                                                "out_scale")]
+
+
+class MLPTrainer(ctypes.Structure):
+    _fields_ = [("max_batch", ctypes.c_int32)] + [(k, ctypes.c_void_p) for k in (
+        "params", "grads", "adam_m", "adam_v", "W1", "W2", "W3", "W4", "W2t", "W3t", "W4t", "Z1", "Z2", "Z3", "Y",
+        "dH", "H1", "H2", "H3", "H1t", "H2t", "H3t", "Xt", "dY", "dZ", "dYt", "dZt", "status")]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -92,6 +107,11 @@ _PROTOS = {
     "ffmpm_substep_adjoint": (ctypes.c_int, [_P(Params), _P(Particles), _P(Adjoint), _vp, ctypes.c_size_t, _vp]),
     "ffmpm_tc_gemm_bf16": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                           ctypes.c_int32, _vp, _vp]),
+    "ffmpm_corrector_g2p": (ctypes.c_int, [_P(Params), _P(Grid), _P(Particles), _vp, _vp, _vp, _vp, _vp]),
+    "ffmpm_mlp_train_forward": (ctypes.c_int, [_P(MLPTrainer), _vp, ctypes.c_int32, _vp]),
+    "ffmpm_mlp_train_backward": (ctypes.c_int, [_P(MLPTrainer), _vp, _vp, ctypes.c_int32, _vp, _vp]),
+    "ffmpm_mlp_train_update": (ctypes.c_int, [_P(MLPTrainer), ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                              ctypes.c_float, ctypes.c_int32, _vp]),
     "ffmpm_version": (ctypes.c_char_p, []),
 }
 

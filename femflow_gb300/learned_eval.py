@@ -1,0 +1,134 @@
+"""Train the learned corrector and measure it against the plain fine-dt and plain coarse-dt forms.
+
+    python -m femflow_gb300.learned_eval [--res 128 --dt 5e-5 --ratio 8 --horizon 50 ...]
+
+1. Data: fine-dt rollouts of ``--scenes`` seeded two-cube scenes (E log-uniform in --E-range, nu in
+   [0.2, 0.35], speeds in [0.5, 1.5], textbook fixed-corotated stress), ``--samples`` sample points
+   each (one coarse step exported, k fine steps as the target).
+2. Training on the tensor cores (``learned.train``).
+3. Selection on a held-out validation scene (its own seed) at the evaluation horizon: the corrected
+   outputs ("v": velocity only, "all": velocity and F) and the strength in {0, 1/4, 1/2, 1}; strength
+   0 (the network off) is always a candidate, so the selected form is never worse than the plain
+   coarse step on the validation scene.
+4. Evaluation on the two-cube scene of 2 x ``--n-per-cube`` particles: plain fine rollout (the
+   judge), plain coarse rollout and the selected corrected rollout with the det F / energy fallback,
+   each timed end to end on the GPU (synchronised wall clock), for the same simulated time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import torch
+
+from . import learned as L
+
+
+def select(net: L.Net, spec: L.SceneSpec, res, dt, ratio, horizon) -> dict:
+    st = L.Stepper(spec, res=res, dt=dt, ratio=ratio)
+    b0 = st.initial_state()
+    fine = b0.clone()
+    L.rollout_fine(st, fine, horizon * ratio)
+    trials = []
+    for mode in ("v", "all"):
+        for a in (0.0, 0.25, 0.5, 1.0):
+            if a == 0.0 and mode == "all":
+                continue
+            cor = L.Corrector(net, st, a)
+            if mode == "v":
+                cor.out_scale[0:9] = 0.0
+            b = b0.clone()
+            for _ in range(horizon):
+                st.coarse_step(b, cor)
+            err = L.position_error(b, fine)["max"]
+            trials.append(dict(mode=mode, strength=a, err_max=err if err == err else float("inf")))
+    best = min(trials, key=lambda t: t["err_max"])
+    return dict(best=best, trials=trials)
+
+
+def corrector_for(net, st, choice):
+    cor = L.Corrector(net, st, choice["strength"])
+    if choice["mode"] == "v":
+        cor.out_scale[0:9] = 0.0
+    return cor
+
+
+def run(res=128, dt=5e-5, ratio=8, scenes=64, per_cube=16384, samples=4, steps=4000, batch=32768, horizon=50,
+        n_per_cube=524288, E_eval=120.0, E_range=(50.0, 200.0), seed=0) -> dict:
+    rep = dict(res=res, dt_fine=dt, ratio=ratio, dt_coarse=dt * ratio, horizon_coarse_steps=horizon,
+               simulated_time=horizon * ratio * dt, E_range=E_range, E_eval=E_eval, model="fixed_corotated")
+    t0 = time.perf_counter()
+    specs = L.training_specs(scenes, per_cube, seed=seed, E_range=E_range)
+    X, T = L.generate(specs, res=res, dt=dt, ratio=ratio, samples_per_scene=samples, warm=20, gap=24)
+    torch.cuda.synchronize()
+    rep["samples"] = int(X.shape[0])
+    rep["data_seconds"] = time.perf_counter() - t0
+    net = L.Net(max_batch=batch, seed=seed)
+    L.fit_scales(net, X, T)
+    Xs, Ts = L.scaled(net, X, T)
+    del X, T
+    nval = min(Xs.shape[0] // 10 // batch * batch, 8 * batch)
+    base = L.evaluate_loss(net, Xs[-nval:], Ts[-nval:], batch)
+    t0 = time.perf_counter()
+    log = L.train(net, Xs[:-nval], Ts[:-nval], steps=steps, batch=batch, lr=2e-3, seed=seed)
+    torch.cuda.synchronize()
+    rep["train_seconds"] = time.perf_counter() - t0
+    rep["train_steps"], rep["batch"] = steps, batch
+    rep["train_loss_log"] = log[:: max(1, len(log) // 10)]
+    rep["val_loss_untrained"] = base
+    rep["val_loss_trained"] = L.evaluate_loss(net, Xs[-nval:], Ts[-nval:], batch)
+    del Xs, Ts
+    val_spec = L.SceneSpec(n_per_cube=per_cube * 2, E=E_eval, nu=0.3, speed=1.0, seed=seed * 1000 + 777)
+    sel = select(net, val_spec, res, dt, ratio, horizon)
+    rep["selection"] = sel
+    # evaluation scene
+    spec = L.SceneSpec(n_per_cube=n_per_cube, E=E_eval, nu=0.3, speed=1.0, seed=seed * 1000 + 999)
+    st = L.Stepper(spec, res=res, dt=dt, ratio=ratio)
+    rep["particles"] = st.n
+    b0 = st.initial_state()
+    for _ in range(2):  # warm-up of every path
+        w = b0.clone()
+        st.fine_step(w)
+        st.coarse_step(w)
+        st.coarse_step(w, corrector_for(net, st, sel["best"]))
+    fine = b0.clone()
+    _, t_fine = L.timed(L.rollout_fine, st, fine, horizon * ratio)
+    plain = b0.clone()
+    info_p, t_plain = L.timed(L.rollout_coarse, st, plain, horizon, None)
+    cor = corrector_for(net, st, sel["best"])
+    learned = b0.clone()
+    info_l, t_learned = L.timed(L.rollout_coarse, st, learned, horizon, cor)
+    st.check()
+    rep["fine"] = dict(seconds=t_fine, substeps=horizon * ratio)
+    rep["plain_coarse"] = dict(seconds=t_plain, error=L.position_error(plain, fine), **info_p)
+    rep["learned"] = dict(seconds=t_learned, error=L.position_error(learned, fine), choice=sel["best"], **info_l)
+    rep["speedup_learned_vs_fine"] = t_fine / t_learned
+    rep["speedup_plain_coarse_vs_fine"] = t_fine / t_plain
+    rep["gain_error_ratio_plain_over_learned"] = rep["plain_coarse"]["error"]["max"] / max(
+        rep["learned"]["error"]["max"], 1e-30)
+    return rep
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--res", type=int, default=128)
+    ap.add_argument("--dt", type=float, default=5e-5)
+    ap.add_argument("--ratio", type=int, default=8)
+    ap.add_argument("--scenes", type=int, default=64)
+    ap.add_argument("--per-cube", type=int, default=16384)
+    ap.add_argument("--samples", type=int, default=4)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--batch", type=int, default=32768)
+    ap.add_argument("--horizon", type=int, default=50)
+    ap.add_argument("--n-per-cube", type=int, default=524288)
+    ap.add_argument("--E", type=float, default=120.0)
+    ap.add_argument("--seed", type=int, default=0)
+    a = ap.parse_args(argv)
+    r = run(a.res, a.dt, a.ratio, a.scenes, a.per_cube, a.samples, a.steps, a.batch, a.horizon, a.n_per_cube, a.E,
+            seed=a.seed)
+    print(json.dumps(r, indent=1, default=float))
+
+
+if __name__ == "__main__":
+    main()

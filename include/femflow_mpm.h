@@ -235,6 +235,82 @@ int ffmpm_substep_adjoint(const ffmpm_params *p, const ffmpm_particles *P, ffmpm
 int ffmpm_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, float *D, int32_t M, int32_t N, int32_t K,
                        int32_t split_k, int32_t *status, void *stream);
 
+/* The corrector network: FFMPM_MLP_FEATURES features (padded to FFMPM_MLP_IN) -> 64 -> 64 -> 64 -> 12 outputs,
+ * GELU between layers.  Weights bf16 row-major [out][in] (W4 padded to 16 rows, zero beyond 12),
+ * biases and scales float32: features are multiplied by in_scale[FFMPM_MLP_IN] before the first
+ * layer, outputs by out_scale[16] after the last. */
+#define FFMPM_MLP_IN 128
+#define FFMPM_MLP_FEATURES 113 /* features in use; the rest of the FFMPM_MLP_IN inputs are zero */
+#define FFMPM_MLP_HIDDEN 64
+#define FFMPM_MLP_OUT 12
+typedef struct ffmpm_mlp {
+  const uint16_t *W1, *W2, *W3, *W4; /* [64][128], [64][64], [64][64], [16][64] */
+  const float *b1, *b2, *b3, *b4;    /* [64], [64], [64], [16] */
+  const float *in_scale, *out_scale; /* [128] (nullable: 1), [16] */
+} ffmpm_mlp;
+
+/* G2P of a coarse 3D substep (float32, dense caller grid after ffmpm_grid_op) fused with the
+ * learned corrector: every particle gathers its 27 nodes, forms v', C', F', x' as three_d.g2p
+ * (g2p.py:9-59), builds its features [F' - I, C' dt, (v' - u) dt/dx, (v_i - u) dt/dx for the 27
+ * nodes, mu k, lam k, PF k with k = dt^2 / (rho dx^2); u = the stencil's centre node velocity, PF
+ * the stress of the pre-step F], and, when `net` is given, runs the network on the
+ * tensor cores and applies F' += y[0:9], v' += y[9:12] dx/dt, x' += dt y[9:12] dx/dt.  The particle
+ * state is updated in place.  features_out (nullable, bf16 [n][FFMPM_MLP_IN], 16-byte aligned)
+ * receives the scaled features.  det_range (nullable, device int32[2], initialise to
+ * {0x7FFFFFFF, 0x80000000}) receives the min / max of det F' as order-preserving keys (k >= 0 ? k :
+ * k ^ 0x7FFFFFFF are the float bits).  status: device int32 (OOB, TIMEOUT bits).  The reference has
+ * no counterpart. */
+int ffmpm_corrector_g2p(const ffmpm_params *p, const ffmpm_grid *grid, ffmpm_particles *P, const ffmpm_mlp *net,
+                        uint16_t *features_out, int32_t *det_range, int32_t *status, void *stream);
+
+/* Training of the corrector network on the tensor cores.  Master parameters, gradients and Adam
+ * moments are float32 in one flat layout of FFMPM_MLP_PARAMS floats:
+ *   W1 at 0 (rows of 128, 64 used), W2 at 16384, W3 at 24576, W4 at 32768 (rows of 64; W2, W3: 64
+ *   rows used; W4: 12), b1 at 40960, b2 at 41024, b3 at 41088, b4 at 41152 (16).
+ * Activation buffers are sized for max_batch rows (a multiple of 128); transposed buffers are
+ * strided by the batch of the call and their padding rows (Xt rows 113.., dYt rows 12.., dZt rows
+ * 64..) are zeroed by the calls themselves.  All buffers are caller allocated. */
+#define FFMPM_MLP_PARAMS 41168
+#define FFMPM_MLP_OFF_W1 0
+#define FFMPM_MLP_OFF_W2 16384
+#define FFMPM_MLP_OFF_W3 24576
+#define FFMPM_MLP_OFF_W4 32768
+#define FFMPM_MLP_OFF_B1 40960
+#define FFMPM_MLP_OFF_B2 41024
+#define FFMPM_MLP_OFF_B3 41088
+#define FFMPM_MLP_OFF_B4 41152
+typedef struct ffmpm_mlp_trainer {
+  int32_t max_batch;
+  float *params, *grads, *adam_m, *adam_v;
+  uint16_t *W1, *W2, *W3, *W4;       /* packed bf16 weights, as ffmpm_mlp */
+  uint16_t *W2t, *W3t, *W4t;         /* [64][64]: W2^T, W3^T, W4^T (zero beyond W4's 12 rows) */
+  float *Z1, *Z2, *Z3;               /* [B][64] pre-activations */
+  float *Y;                          /* [B][16] */
+  float *dH;                         /* [B][64] */
+  uint16_t *H1, *H2, *H3;            /* [B][64] */
+  uint16_t *H1t, *H2t, *H3t;         /* [64][B] */
+  uint16_t *Xt;                      /* [128][B] */
+  uint16_t *dY, *dZ;                 /* [B][64] */
+  uint16_t *dYt, *dZt;               /* [128][B] */
+  int32_t *status;                   /* device int32 (TIMEOUT bit from the tensor-core waits) */
+} ffmpm_mlp_trainer;
+
+/* Forward pass of `batch` rows of bf16 features X [batch][FFMPM_MLP_IN] (16-byte aligned) with the
+ * packed weights and the biases in params: keeps Z1..Z3, H1..H3 (and their transposes, and Xt) and
+ * leaves the network output (before out_scale) in Y. */
+int ffmpm_mlp_train_forward(const ffmpm_mlp_trainer *t, const uint16_t *X, int32_t batch, void *stream);
+
+/* Loss sum_b sum_j w[j] (Y[b][j] - T[b][j])^2 / batch over the 12 outputs (T: float32 [batch][12],
+ * w: float32 [12]), ADDED to *loss (device double), and its gradient with respect to every
+ * parameter written to grads (overwritten).  Needs the preceding ffmpm_mlp_train_forward. */
+int ffmpm_mlp_train_backward(const ffmpm_mlp_trainer *t, const float *T, const float *w, int32_t batch,
+                             double *loss, void *stream);
+
+/* One Adam step (learning rate lr, betas b1 b2, eps; `step` counts from 1) on params, then repack
+ * the bf16 weights W1..W4 and their transposes. */
+int ffmpm_mlp_train_update(const ffmpm_mlp_trainer *t, float lr, float beta1, float beta2, float eps, int32_t step,
+                           void *stream);
+
 /* Library version string. */
 const char *ffmpm_version(void);
 

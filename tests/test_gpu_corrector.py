@@ -1,0 +1,152 @@
+"""Learned corrector on the GPU: tensor-core training pass against the numpy oracle, the fused
+G2P + network kernel against the unfused tensor-core forward, and its plain mode against the
+standard G2P."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import mlp as M
+from femflow_gb300 import _native as N
+from femflow_gb300 import engine as E
+from femflow_gb300 import learned as L
+
+pytestmark = pytest.mark.gpu
+
+
+def _features(rng, B):
+    X = np.zeros((B, 128), dtype=np.float32)
+    X[:, :102] = rng.normal(0, 1, (B, 102))
+    return torch.from_numpy(X).to(torch.bfloat16).cuda()
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def test_training_pass_matches_oracle():
+    rng = np.random.default_rng(0)
+    B = 1024
+    net = L.Net(max_batch=B, seed=1)
+    with torch.no_grad():
+        net.params[M.OFF["b1"]:M.OFF["b1"] + 64] = torch.tensor(rng.normal(0, 0.1, 64), dtype=torch.float32)
+        net.params[M.OFF["b4"]:M.OFF["b4"] + 12] = torch.tensor(rng.normal(0, 0.1, 12), dtype=torch.float32)
+    net.repack()
+    X = _features(rng, B)
+    T = torch.tensor(rng.normal(0, 1, (B, 12)), dtype=torch.float32, device="cuda")
+    w = torch.tensor(rng.uniform(0.5, 2.0, 12), dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    Y = net.forward_train(X).cpu().numpy()
+    net.backward_train(T, w, loss)
+    net.check()
+    P = net.params.cpu().numpy()
+    l_ref, g_ref, Y_ref = M.backward(P, X.float().cpu().numpy(), T.cpu().numpy(), w.cpu().numpy())
+    assert _rel(Y, Y_ref) < 1e-3
+    assert abs(float(loss.item()) - l_ref) <= 1e-3 * l_ref
+    g = net.grads.cpu().numpy()
+    for k, n in (("W1", 64 * 128), ("W2", 4096), ("W3", 4096), ("W4", 768), ("b1", 64), ("b2", 64), ("b3", 64),
+                 ("b4", 12)):
+        sl = slice(M.OFF[k], M.OFF[k] + n)
+        assert _rel(g[sl], g_ref[sl]) < 1e-2, k
+    # padding stays out of the gradient: W1 columns >= 113 and W4 rows >= 12
+    assert np.all(g[0:64 * 128].reshape(64, 128)[:, N.MLP_FEATURES:] == 0)
+    assert np.all(g[M.OFF["W4"] + 768:M.OFF["W4"] + 16 * 64] == 0)
+
+
+def test_adam_update_moves_towards_lower_loss():
+    rng = np.random.default_rng(3)
+    B = 2048
+    net = L.Net(max_batch=B, seed=2)
+    X = _features(rng, B)
+    T = torch.tensor(rng.normal(0, 1, (B, 12)), dtype=torch.float32, device="cuda") * 0.1
+    w = torch.ones(12, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    first = None
+    for it in range(200):
+        loss.zero_()
+        net.forward_train(X)
+        net.backward_train(T, w, loss)
+        net.update(3e-3)
+        if first is None:
+            first = float(loss.item())
+    assert float(loss.item()) < 0.5 * first
+
+
+def _stepper(n_per_cube=8192):
+    return L.Stepper(L.SceneSpec(n_per_cube=n_per_cube, E=100.0), res=64, dt=1e-4, ratio=8)
+
+
+def test_plain_corrector_g2p_matches_standard_g2p():
+    st = _stepper()
+    buf = st.initial_state()
+    for _ in range(5):
+        st.fine_step(buf)
+    # one coarse P2G + grid update, then both G2Ps on copies
+    P = st._P(buf)
+    st.gv.zero_()
+    st.gm.zero_()
+    g = E.grid_struct(st.gv, st.gm)
+    s = st._stream()
+    N.call("ffmpm_p2g", ctypes.byref(st.coarse), ctypes.byref(P), ctypes.byref(g), ctypes.c_void_p(st.ws.ptr),
+           ctypes.c_size_t(st.ws.bytes), s)
+    N.call("ffmpm_grid_op", ctypes.byref(st.coarse), ctypes.byref(g), s)
+    a, b = buf.clone(), buf.clone()
+    Pa, Pb = st._P(a), st._P(b)
+    N.call("ffmpm_g2p", ctypes.byref(st.coarse), ctypes.byref(g), ctypes.byref(Pa), ctypes.c_void_p(st.ws.ptr),
+           ctypes.c_size_t(st.ws.bytes), s)
+    N.call("ffmpm_corrector_g2p", ctypes.byref(st.coarse), ctypes.byref(g), ctypes.byref(Pb), None, None, None,
+           ctypes.c_void_p(st.status.data_ptr()), s)
+    st.check()
+    for r0, r1, tol in ((0, 3, 1e-6), (3, 6, 1e-5), (6, 15, 1e-5), (15, 24, 1e-4)):
+        d = float((a[r0:r1] - b[r0:r1]).abs().max())
+        scale = float(a[r0:r1].abs().max())
+        assert d <= tol * max(scale, 1e-6), (r0, d, scale)
+
+
+def test_fused_corrector_matches_unfused_forward():
+    st = _stepper()
+    buf = st.initial_state()
+    for _ in range(5):
+        st.fine_step(buf)
+    net = L.Net(max_batch=st.n, seed=4)
+    net.in_scale.fill_(0.5)
+    net.out_scale[:12] = 1e-3
+    plain, corr = buf.clone(), buf.clone()
+    X = torch.empty((st.n, 128), dtype=torch.bfloat16, device="cuda")
+    st.coarse_step(plain, None, X)
+    st.reset_det()
+    st.coarse_step(corr, net)
+    st.check()
+    y = net.forward_train(X) * net.out_scale[:12]
+    vs = st.dt * st.ratio * st.res
+    F_exp = plain[6:15] + y[:, :9].t()
+    v_exp = plain[3:6] + y[:, 9:12].t() / vs
+    x_exp = plain[0:3] + st.dt * st.ratio * y[:, 9:12].t() / vs
+    assert float((corr[6:15] - F_exp).abs().max()) <= 1e-6
+    assert float((corr[3:6] - v_exp).abs().max()) <= 1e-5 * float(v_exp.abs().max())
+    assert float((corr[0:3] - x_exp).abs().max()) <= 1e-6
+    # C is not corrected; the two coarse P2Gs differ only in atomic summation order, which moves C by
+    # float32 rounding of the node velocities times 4 / dx
+    c_tol = 1e-6 * 4 * st.res * float(plain[3:6].abs().max())
+    assert float((corr[15:24] - plain[15:24]).abs().max()) <= c_tol
+    lo, hi = st.det_range()
+    J = torch.linalg.det(L.unpack(corr)[2].double())
+    assert abs(lo - float(J.min())) < 1e-4 and abs(hi - float(J.max())) < 1e-4
+
+
+def test_learned_corrector_small_end_to_end():
+    """Data from fine rollouts, tensor-core training, selection on a held-out scene and the timed
+    comparison with the plain fine and plain coarse rollouts (small: 2 x 32,768 particles, 64^3)."""
+    from femflow_gb300 import learned_eval as LE
+    r = LE.run(res=64, dt=1e-4, ratio=8, scenes=16, per_cube=8192, samples=4, steps=800, batch=16384, horizon=25,
+               n_per_cube=32768, E_eval=120.0)
+    assert r["val_loss_trained"] < 0.8 * r["val_loss_untrained"], r
+    sel = r["selection"]
+    plain_val = [t for t in sel["trials"] if t["strength"] == 0.0][0]["err_max"]
+    assert sel["best"]["err_max"] <= plain_val
+    # what the network gains (or not) on the evaluation scene, and the cost of the coarse form
+    print("gain (plain coarse error / learned error):", r["gain_error_ratio_plain_over_learned"],
+          "speedup vs fine:", r["speedup_learned_vs_fine"])
+    assert r["learned"]["error"]["max"] <= 2.0 * r["plain_coarse"]["error"]["max"]
+    assert r["speedup_plain_coarse_vs_fine"] > 1.5
