@@ -277,8 +277,9 @@ __device__ __forceinline__ int tile_nodes(const Geom<DIM>& g) {
 // F - R = F (I - S^-1) = F Y (I + Y)^-1, and Y = S - I is the fixed point of Y = (E - Y^2) / 2 with
 // E = F^T F - I = H + H^T + H^T H, H = F - I.  Every quantity is of the size of the strain, so F - R
 // keeps float's relative precision; Newton's R has an absolute error of ~1e-7, which at strain 1e-4
-// leaves F - R with three correct digits.  Applies when max |E| <= 0.05 (then |Y| < 0.1 and eight
-// iterations reach float precision); returns false otherwise.
+// leaves F - R with three correct digits.  Applies when max |E| <= 0.05 (then |Y|_F < 0.08, the
+// iteration contracts by that factor, and six iterations reach float precision); returns false
+// otherwise.
 template <typename T>
 __device__ __forceinline__ bool f_minus_r_small_strain3(const T F[9], T FmR[9]) {
   T H[9];
@@ -299,7 +300,7 @@ __device__ __forceinline__ bool f_minus_r_small_strain3(const T F[9], T FmR[9]) 
 #pragma unroll
   for (int i = 0; i < 9; ++i) Y[i] = T(0.5) * E[i];
 #pragma unroll
-  for (int it = 0; it < 8; ++it) {
+  for (int it = 0; it < 6; ++it) {
     T Yn[9];
 #pragma unroll
     for (int a = 0; a < 3; ++a)

@@ -12,7 +12,10 @@
    coarse step on the validation scene.
 4. Evaluation on the two-cube scene of 2 x ``--n-per-cube`` particles: plain fine rollout (the
    judge), plain coarse rollout and the selected corrected rollout with the det F / energy fallback,
-   each timed end to end on the GPU (synchronised wall clock), for the same simulated time.
+   each timed end to end on the GPU (synchronised wall clock), for the same simulated time.  The
+   fine and the plain coarse forms are also timed on the resident block-sorted solver (all substeps in
+   one call; the fastest form of each), and the corrected form runs there too when the selected
+   strength is 0 (the network off).
 """
 from __future__ import annotations
 
@@ -100,6 +103,38 @@ def run(res=128, dt=5e-5, ratio=8, scenes=64, per_cube=16384, samples=4, steps=4
     learned = b0.clone()
     info_l, t_learned = L.timed(L.rollout_coarse, st, learned, horizon, cor)
     st.check()
+    # fastest forms: the resident block-sorted solver, CUDA-graph replay, same scene and material
+    from .solver import MPMSolver
+    s = st.scene
+
+    def solver(dt_):
+        return MPMSolver(torch.tensor(s["x"], dtype=torch.float32), res=res, dt=dt_, gravity=-9.8, volume=s["vol"],
+                         mass=s["mass"], mu_0=s["mu"], lambda_0=s["lam"], v=torch.tensor(s["v"]),
+                         dtype=torch.float32, device="cuda", model="fixed_corotated")
+
+    def fast(dt_, steps):
+        solver(dt_).step(2)  # first-call set-up on a throwaway instance
+        sv = solver(dt_)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sv.step(steps)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        sv.check()
+        return sv, t
+
+    sf, t_fine_fast = fast(dt, horizon * ratio)
+    sc, t_coarse_fast = fast(dt * ratio, horizon)
+    xf, xc = sf.positions(), sc.positions()
+    err_fast = (xc - xf).abs()
+    rep["fine_fast"] = dict(seconds=t_fine_fast, substeps=horizon * ratio)
+    rep["plain_coarse_fast"] = dict(seconds=t_coarse_fast, error=dict(max=float(err_fast.max()),
+                                                                      mean=float(err_fast.mean())))
+    rep["speedup_plain_coarse_fast_vs_fine_fast"] = t_fine_fast / t_coarse_fast
+    if sel["best"]["strength"] == 0.0:
+        rep["learned_fast"] = dict(note="selected strength 0: the corrected form is the plain coarse form",
+                                   seconds=t_coarse_fast)
+        rep["speedup_learned_fast_vs_fine_fast"] = t_fine_fast / t_coarse_fast
     rep["fine"] = dict(seconds=t_fine, substeps=horizon * ratio)
     rep["plain_coarse"] = dict(seconds=t_plain, error=L.position_error(plain, fine), **info_p)
     rep["learned"] = dict(seconds=t_learned, error=L.position_error(learned, fine), choice=sel["best"], **info_l)
