@@ -41,6 +41,7 @@ UNIT = "particle-substeps/s"
 N_PER_CUBE = 524_288
 RES, DT, GRAVITY, E_YOUNG, NU, EDGE = 128, 5e-5, -9.8, 4.5e3, 0.3, 0.2
 WORKLOAD = "two_cubes_1M_res128"
+SORT_EVERY = 8  # substeps between re-sorts by block (earlier when a particle leaves its block's neighbourhood)
 
 
 def scene(seed: int = 0):
@@ -159,7 +160,8 @@ def run_ours(args):
     clocks = ClockSampler(bus if isinstance(bus, str) else None)
 
     solver = MPMSolver(torch.tensor(s["x"]), res=RES, dt=DT, gravity=GRAVITY, volume=s["vol"], mass=s["mass"],
-                       mu_0=s["mu"], lambda_0=s["lam"], v=torch.tensor(s["v"]), dtype=torch.float32, device=dev)
+                       mu_0=s["mu"], lambda_0=s["lam"], v=torch.tensor(s["v"]), dtype=torch.float32, device=dev,
+                       sort_every=SORT_EVERY)
     info = solver.plan_info()
     solver.step(args.warmup)
     torch.cuda.synchronize(dev)
@@ -195,7 +197,7 @@ def run_ours(args):
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded two-cube scene)",
            "config": config({"parallelism": f"replicas{world}" if world > 1 else "single GPU",
                              "cuda_graph_substeps": gsteps, "radix_passes": info["radix_passes"],
-                             "block_size": info["block_size"]}),
+                             "block_size": info["block_size"], "sort_every": SORT_EVERY}),
            "clocks": clocks.summary(t_wall0, t_wall1), "gpu_launches": int(gpu_launches),
            "status": {"device_status": status, "polar_fp64_fallbacks": fallbacks}}
 

@@ -59,6 +59,8 @@ bool make_layout(const ffmpm_params& p, int64_t n, Layout* L) {
   L->nblocks = p.dim == 3 ? int64_t(L->nb) * L->nb * L->nb : int64_t(L->nb) * L->nb;
   L->nnodes = p.dim == 3 ? int64_t(L->R) * L->R * L->R : int64_t(L->R) * L->R;
   // keys order particles by block, then by cell inside the block
+  // keys order particles by block, then by cell inside the block, so that each P2G chunk spans few
+  // cells (between re-sorts the P2G regroups each chunk by cell itself)
   L->cell_bits = p.dim * ilog2_ceil(L->bs);
   L->key_bits = ilog2_ceil(L->nblocks) + L->cell_bits;
   if (L->key_bits > 31) return false;
@@ -238,10 +240,26 @@ struct PhaseTimer {
   }
 };
 
-// keys -> sort -> plan.  Leaves the permutation pointer in *perm.
+// Substeps between re-sorts (ffmpm_params.variant bits 8..15; 0 or 1: every substep).  The
+// deterministic mode always re-sorts (its per-block CTAs need every particle in its block).
+int sort_every(const ffmpm_params& p) {
+  const int k = (p.variant >> kVariantSortShift) & 0xFF;
+  return (p.deterministic || k < 1) ? 1 : k;
+}
+
+// Start of a substep of a cadenced run: re-sort when the cadence says so or when the previous
+// G2P saw a particle leave the neighbourhood its block's plan covers.
+__global__ void k_sort_decide(WsHeader* h, int periodic) {
+  h->sort_now = (periodic || h->far_stray) ? 1u : 0u;
+  h->far_stray = 0u;
+}
+
+// keys -> sort -> plan.  Leaves the permutation pointer in *perm.  With `flag` (cadenced runs) the
+// sort and the plan do their work only when the device word reads 1, and the plan dilates the
+// occupied blocks by +-1 so that it stays valid until the next re-sort.
 template <int DIM, typename T>
 void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<T>& x, bool keys_ready,
-                   const uint32_t** perm, cudaStream_t s, PhaseTimer* tm = nullptr) {
+                   const uint32_t** perm, cudaStream_t s, PhaseTimer* tm = nullptr, const uint32_t* flag = nullptr) {
   const KParams<T> kp = kparams<T>(p);
   const Geom<DIM> g = geom<DIM>(L);
   const uint32_t n = (uint32_t)L.n;
@@ -253,11 +271,12 @@ void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const PV
   }
   const uint32_t* ks = nullptr;
   if (tm) tm->begin(1);
-  radix_sort(w.keys_next, n, L.passes, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, &w.hdr->status, s, &ks, perm);
+  radix_sort(w.keys_next, n, L.passes, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, &w.hdr->status, s,
+             &ks, perm, flag);
   if (tm) tm->end(1 + L.passes);
   if (tm) tm->begin(2);
   k_plan<DIM><<<1, 1024, 0, s>>>(g, w.block_count, w.block_start, w.block_cnt, w.chunks, w.touched, w.occupied,
-                                 w.hdr);
+                                 w.hdr, flag, flag ? 1 : 0);
   if (tm) tm->end(1);
 }
 
@@ -281,17 +300,19 @@ void set_smem(F* kernel, size_t bytes) {
 
 template <int DIM, typename T, typename Sink>
 void launch_p2g(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<T>& P, const uint32_t* perm,
-                const Sink& sink, cudaStream_t s) {
-  const bool direct = (p.variant & kVariantP2GDirect) != 0;
-  const bool lanes = (p.variant & kVariantP2GLanes) != 0;
+                const Sink& sink, cudaStream_t s, const uint32_t* flag = nullptr) {
+  // plans kept over several substeps need the stray path of the cell-run kernel
+  const bool direct = !flag && (p.variant & kVariantP2GDirect) != 0;
+  const bool lanes = !flag && (p.variant & kVariantP2GLanes) != 0;
   if (!direct && !lanes) {
     // default: cell-run P2G (tile + per-particle records + cell ids + run starts)
+    const int ncell = DIM == 3 ? L.bs * L.bs * L.bs : L.bs * L.bs;
     const size_t smem = tile_smem<DIM, T>(L) + size_t(kChunk) * RecLayout<DIM>::kStride * sizeof(T) +
-                        sizeof(int) * (2 * kChunk + 1);
+                        sizeof(int) * (3 * kChunk + std::max(kChunk, ncell) + 1 + ncell);
     auto kern = k_p2g_cells<DIM, T, Sink>;
     set_smem(kern, smem);
     kern<<<work_grid(L.max_chunks, resident_per_sm(kern, smem)), kThreads, smem, s>>>(
-        kparams<T>(p), geom<DIM>(L), P, perm, w.chunks, w.hdr, sink, &w.hdr->status, &w.hdr->polar_fallbacks);
+        kparams<T>(p), geom<DIM>(L), P, perm, w.chunks, w.hdr, sink, &w.hdr->status, &w.hdr->polar_fallbacks, flag);
     return;
   }
   const size_t smem = direct ? 0 : tile_smem<DIM, T>(L);
@@ -329,7 +350,8 @@ void launch_grid_update(const ffmpm_params& p, const Layout& L, const Ws& w, cud
 
 template <int DIM, typename T, bool kTma, bool kSorted>
 int launch_g2p(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<T>& Pin, const PView<T>& Pout,
-               const uint32_t* perm, const T* user_gv, const G2PExtra& ex, cudaStream_t s) {
+               const uint32_t* perm, const T* user_gv, const G2PExtra& ex, cudaStream_t s,
+               const uint32_t* flag = nullptr) {
   alignas(64) CUtensorMap map;
   std::memset(&map, 0, sizeof(map));
   if (kTma && !encode_grid_map(&map, w.gridB, L)) return FFMPM_ERR_CUDA;
@@ -337,7 +359,7 @@ int launch_g2p(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<
   auto kern = k_g2p<DIM, T, kTma, kSorted>;
   set_smem(kern, smem);
   kern<<<work_grid(L.max_chunks, resident_per_sm(kern, smem)), kThreads, smem, s>>>(
-      kparams<T>(p), geom<DIM>(L), Pin, Pout, perm, w.chunks, w.hdr, map, user_gv, ex, &w.hdr->status);
+      kparams<T>(p), geom<DIM>(L), Pin, Pout, perm, w.chunks, w.hdr, map, user_gv, ex, &w.hdr->status, flag);
   return FFMPM_OK;
 }
 
@@ -363,18 +385,21 @@ template <int DIM, typename T>
 int op_substeps_sorted(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_particles* a, ffmpm_particles* b,
                        int32_t* ids_a, int32_t* ids_b, int nsteps, cudaStream_t s, PhaseTimer* tm = nullptr) {
   PView<T> va = pview<T>(*a), vb = pview<T>(*b);
+  const int K = sort_every(p);
+  const uint32_t* flag = K > 1 ? &w.hdr->sort_now : nullptr;
   for (int k = 0; k < nsteps; ++k) {
     const PView<T>& in = (k & 1) ? vb : va;
     const PView<T>& out = (k & 1) ? va : vb;
     const int32_t* ids_in = (k & 1) ? ids_b : ids_a;
     int32_t* ids_out = (k & 1) ? ids_a : ids_b;
     const uint32_t* perm = nullptr;
-    sort_and_plan<DIM, T>(p, L, w, in, k > 0, &perm, s, tm);
+    if (flag) k_sort_decide<<<1, 1, 0, s>>>(w.hdr, k % K == 0 ? 1 : 0);
+    sort_and_plan<DIM, T>(p, L, w, in, k > 0, &perm, s, tm, flag);
     if (tm) tm->begin(3);
     if (p.deterministic)
       launch_p2g_det<DIM, T>(p, L, w, in, perm, s);
     else
-      launch_p2g<DIM, T>(p, L, w, in, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s);
+      launch_p2g<DIM, T>(p, L, w, in, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s, flag);
     if (tm) tm->end(1);
     if (tm) tm->begin(4);
     if (p.deterministic)
@@ -382,9 +407,10 @@ int op_substeps_sorted(const ffmpm_params& p, const Layout& L, const Ws& w, ffmp
     else
       launch_grid_update<DIM, T>(p, L, w, s);
     if (tm) tm->end(1);
-    G2PExtra ex{ids_in, ids_out, w.keys_next, w.block_count, L.cell_bits};
+    G2PExtra ex{ids_in, ids_out, w.keys_next, w.block_count, L.cell_bits, flag ? w.gridB : nullptr,
+                flag ? &w.hdr->far_stray : nullptr};
     if (tm) tm->begin(5);
-    int rc = launch_g2p<DIM, T, true, true>(p, L, w, in, out, perm, nullptr, ex, s);
+    int rc = launch_g2p<DIM, T, true, true>(p, L, w, in, out, perm, nullptr, ex, s, flag);
     if (tm) tm->end(1);
     if (rc != FFMPM_OK) return rc;
   }
@@ -603,7 +629,9 @@ int ffmpm_plan_info(const ffmpm_params* p, int64_t n, int64_t* info) {
   info[2] = L.nblocks;
   info[3] = L.key_bits;
   info[4] = L.passes;
-  info[5] = L.passes + 5;  // digit histogram + one kernel per radix pass + plan + P2G + grid + G2P
+  // digit histogram + one kernel per radix pass + plan + P2G + grid + G2P (+ the re-sort decision
+  // of cadenced runs)
+  info[5] = L.passes + 5 + (sort_every(*p) > 1 ? 1 : 0);
   info[6] = L.tile;
   info[7] = L.max_chunks;
   return FFMPM_OK;

@@ -21,7 +21,9 @@ struct WsHeader {
   uint32_t n_touched;
   uint32_t n_occupied;
   uint32_t n_valid;
-  uint32_t pad[58];
+  uint32_t sort_now;   // sort cadence: 1 when this substep re-sorts (set by k_sort_decide)
+  uint32_t far_stray;  // set by G2P when a particle left the neighbourhood its block's plan covers
+  uint32_t pad[56];
 };
 static_assert(sizeof(WsHeader) == 256, "header is one 256-byte line");
 
@@ -41,11 +43,12 @@ int sm_count();
 
 // Radix sort (sort.cu): stable, 8-bit digits, `passes` passes over keys_in (n keys); values start
 // as the identity permutation.  `scratch` holds radix_scratch_words(passes, ntiles) words (zeroed
-// by the call).  Returns the buffers that hold the sorted keys / permutation.
+// by the call).  Returns the buffers that hold the sorted keys / permutation.  With `sort_flag`
+// (device word, nullable) the kernels do nothing when it reads 0.
 constexpr int kMaxRadixPasses = 4;
 size_t radix_scratch_words(int passes, int64_t ntiles);
 void radix_sort(const uint32_t* keys_in, uint32_t n, int passes, uint32_t* keys0, uint32_t* keys1, uint32_t* vals0,
                 uint32_t* vals1, uint32_t* scratch, int ntiles, int32_t* status, cudaStream_t s,
-                const uint32_t** keys_sorted, const uint32_t** perm);
+                const uint32_t** keys_sorted, const uint32_t** perm, const uint32_t* sort_flag = nullptr);
 
 }  // namespace ffmpm

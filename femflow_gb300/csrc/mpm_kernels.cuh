@@ -29,6 +29,7 @@ struct KParams {
 // Variant flags (ffmpm_params.variant).
 constexpr int kVariantP2GDirect = 1;  // P2G scatters straight to L2 with vector reds (no smem tile)
 constexpr int kVariantP2GLanes = 2;   // P2G lane-per-particle shared-tile atomics (no cell runs)
+constexpr int kVariantSortShift = 8;  // bits 8..15: substeps between re-sorts of the sorted solver
 
 template <typename T>
 struct PView {
@@ -189,7 +190,13 @@ template <int DIM>
 __global__ void __launch_bounds__(1024) k_plan(Geom<DIM> g, uint32_t* __restrict__ block_count,
                                                uint32_t* __restrict__ block_start, uint32_t* __restrict__ block_cnt,
                                                int4* __restrict__ chunks, uint32_t* __restrict__ touched,
-                                               int4* __restrict__ occupied, WsHeader* hdr) {
+                                               int4* __restrict__ occupied, WsHeader* hdr,
+                                               const uint32_t* __restrict__ sort_flag, int sym) {
+  if (sort_flag && *sort_flag == 0u) {
+    // no re-sort this substep: keep the plan, only clear the histogram G2P accumulates
+    for (int b = threadIdx.x; b < g.nblocks; b += blockDim.x) block_count[b] = 0;
+    return;
+  }
   __shared__ Scan4 warp_buf[32];
   Scan4 carry{0, 0, 0, 0};  // (particles, chunks, touched, occupied)
   for (int seg = 0; seg < g.nblocks; seg += blockDim.x) {
@@ -199,18 +206,46 @@ __global__ void __launch_bounds__(1024) k_plan(Geom<DIM> g, uint32_t* __restrict
       c = block_count[b];
       int bc[DIM];
       block_coords<DIM>(g, b, bc);
-      // touched if any block b - o, o in {0,1}^DIM, holds particles
+      // touched if any block b - o, o in {0,1}^DIM, holds particles; with `sym` (plans kept over
+      // several substeps) any block b + o, o in {-1,0,1}^DIM
+      if (!sym) {
 #pragma unroll
-      for (int o = 0; o < (1 << DIM); ++o) {
-        int nb_id = 0;
-        bool ok = true;
+        for (int o = 0; o < (1 << DIM); ++o) {
+          int nb_id = 0;
+          bool ok = true;
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          const int cc = bc[d] - ((o >> (DIM - 1 - d)) & 1);
-          ok = ok && cc >= 0;
-          nb_id = nb_id * g.nb + cc;
+          for (int d = 0; d < DIM; ++d) {
+            const int cc = bc[d] - ((o >> (DIM - 1 - d)) & 1);
+            ok = ok && cc >= 0;
+            nb_id = nb_id * g.nb + cc;
+          }
+          if (ok && block_count[nb_id] > 0) tch = 1;
         }
-        if (ok && block_count[nb_id] > 0) tch = 1;
+      } else {
+        constexpr int NO = DIM == 3 ? 27 : 9;
+        for (int o = 0; o < NO; ++o) {
+          int nb_id = 0, r = o;
+          bool ok = true;
+#pragma unroll
+          for (int d = DIM - 1; d >= 0; --d) {
+            const int cc = bc[d] + (r % 3) - 1;
+            r /= 3;
+            ok = ok && cc >= 0 && cc < g.nb;
+          }
+          if (!ok) continue;
+          r = o;
+          int mul = 1;
+#pragma unroll
+          for (int d = DIM - 1; d >= 0; --d) {
+            nb_id += (bc[d] + (r % 3) - 1) * mul;
+            mul *= g.nb;
+            r /= 3;
+          }
+          if (block_count[nb_id] > 0) {
+            tch = 1;
+            break;
+          }
+        }
       }
     }
     const uint32_t nch = (c + kChunk - 1) / kChunk;
@@ -561,20 +596,26 @@ __device__ __forceinline__ void p2g_load(const KParams<T>& kp, const PView<T>& P
   in.jp = kp.model == FFMPM_MODEL_SNOW ? P.Jp[p] : T(1);
 }
 
+// Record of one particle.  Returns kRecTile when its stencil lies in the chunk block's tile,
+// kRecStray when it is inside the grid but its stencil left that tile (possible between re-sorts;
+// the record is complete and base[] holds its base node), kRecOut when it is outside the grid.
+constexpr int kRecOut = 0, kRecTile = 1, kRecStray = 2;
+
 template <int DIM, typename T>
-__device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>& g, const P2GIn<DIM, T>& in,
-                                           const int org[DIM], T* rec, int& cell, int32_t* status,
-                                           uint32_t* fallbacks) {
+__device__ __forceinline__ int p2g_record(const KParams<T>& kp, const Geom<DIM>& g, const P2GIn<DIM, T>& in,
+                                          const int org[DIM], T* rec, int& cell, int32_t* status,
+                                          uint32_t* fallbacks, int base[DIM]) {
   constexpr int DD = DIM * DIM;
   T fx[DIM], w[3][DIM];
   int lb[DIM];
-  bool ok = true;
+  bool ok = true, in_tile = true;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     int b;
     ok = ok && base_of(in.x[d], kp.inv_dx, kp.res, b, fx[d]);
+    base[d] = b;
     lb[d] = b - org[d];
-    ok = ok && lb[d] >= 0 && lb[d] + 2 < g.tile;
+    in_tile = in_tile && lb[d] >= 0 && lb[d] + 2 < g.tile;
     T ww[3];
     bspline(fx[d], ww);
     w[0][d] = ww[0];
@@ -583,9 +624,9 @@ __device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>
   }
   if (!ok) {
     raise_status(status, FFMPM_STATUS_OOB);
-    return false;
+    return kRecOut;
   }
-  cell = DIM == 3 ? (lb[0] * g.bs + lb[1]) * g.bs + lb[2] : lb[0] * g.bs + lb[1];
+  cell = in_tile ? (DIM == 3 ? (lb[0] * g.bs + lb[1]) * g.bs + lb[2] : lb[0] * g.bs + lb[1]) : -1;
   const T m = in.m;
   const T e = (kp.model == FFMPM_MODEL_SNOW) ? ffexp(kp.hardening * (T(1) - in.jp)) : kp.hardening;
   T A[DD];
@@ -607,7 +648,32 @@ __device__ __forceinline__ bool p2g_record(const KParams<T>& kp, const Geom<DIM>
   for (int d = 0; d < DIM; ++d)
 #pragma unroll
     for (int i = 0; i < 3; ++i) rec[w0 + 3 * d + i] = w[i][d];
-  return true;
+  return in_tile ? kRecTile : kRecStray;
+}
+
+// Scatter one record straight to the global grid through the sink (a particle whose stencil left
+// its chunk block's tile): node (i, j[, k]) gets w (q + dx A (i, j[, k])) and w m.
+template <int DIM, typename T, typename Sink>
+__device__ __noinline__ void p2g_scatter_record(const T* rec, const int base[DIM], int R, const Sink& sink) {
+  constexpr int a0 = 1 + DIM;
+  constexpr int w0 = RecLayout<DIM>::kW;
+  const T m = rec[0];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < (DIM == 3 ? 3 : 1); ++k) {
+        const int o[3] = {i, j, k};
+        T wt = rec[w0 + i] * rec[w0 + 3 + j];
+        if constexpr (DIM == 3) wt *= rec[w0 + 6 + k];
+        T q[3] = {T(0), T(0), T(0)};
+        for (int r = 0; r < DIM; ++r) {
+          T a = rec[1 + r];
+          for (int c = 0; c < DIM; ++c) a += rec[a0 + r * DIM + c] * T(o[c]);
+          q[r] = wt * a;
+        }
+        int I[DIM];
+        for (int d = 0; d < DIM; ++d) I[d] = base[d] + o[d];
+        sink.add(node_index<DIM>(R, I), q[0], q[1], DIM == 3 ? q[2] : T(0), wt * m);
+      }
 }
 
 template <int DIM, typename T, typename Sink>
@@ -615,7 +681,8 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
                                                         const uint32_t* __restrict__ perm,
                                                         const int4* __restrict__ chunks,
                                                         const WsHeader* __restrict__ hdr, Sink sink, int32_t* status,
-                                                        uint32_t* fallbacks) {
+                                                        uint32_t* fallbacks, const uint32_t* __restrict__ sort_flag) {
+  if (sort_flag && *sort_flag == 0u) perm = nullptr;  // plan kept from an earlier substep: identity order
   constexpr int RF = RecLayout<DIM>::kFloats;
   constexpr int RS = RecLayout<DIM>::kStride;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -623,9 +690,14 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
   T* tile = reinterpret_cast<T*>(smem_raw);
   T* recs = tile + 4 * TN;                                          // [kChunk][RS]
   int* cells = reinterpret_cast<int*>(recs + (size_t)kChunk * RS);  // [kChunk]
-  int* runs = cells + kChunk;                                       // [kChunk + 1]
+  const int ncell = DIM == 3 ? g.bs * g.bs * g.bs : g.bs * g.bs;
+  int* rank = cells + kChunk;                                       // [kChunk]
+  int* order = rank + kChunk;                                       // [kChunk]
+  int* runs = order + kChunk;                                       // [max(kChunk, ncell) + 1]
+  int* hist = runs + max(kChunk, ncell) + 1;                        // [ncell]
   __shared__ int nruns_s;
   __shared__ int warp_cnt[kThreads / 32];
+  __shared__ int warp_nz[kThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t nch = hdr->n_chunks;
   const uint32_t per = (nch + gridDim.x - 1) / gridDim.x;
@@ -654,7 +726,8 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
     for (int l = threadIdx.x; l < ch.z; l += 2 * blockDim.x) {
       const int l2 = l + blockDim.x;
       const bool two = l2 < ch.z;
-      const uint32_t p1 = perm[ch.y + l], p2 = perm[ch.y + (two ? l2 : l)];
+      const uint32_t s1 = ch.y + l, s2 = ch.y + (two ? l2 : l);
+      const uint32_t p1 = perm ? perm[s1] : s1, p2 = perm ? perm[s2] : s2;
       P2GIn<DIM, T> in[2];
       p2g_load<DIM, T>(kp, P, p1, in[0]);
       p2g_load<DIM, T>(kp, P, p2, in[1]);
@@ -663,8 +736,10 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
         if (u == 1 && !two) break;
         const int lu = u ? l2 : l;
         T rec[RS];
-        int cell = -1;
-        if (!p2g_record<DIM, T>(kp, g, in[u], org, rec, cell, status, fallbacks)) cell = -1;
+        int cell = -1, base[DIM];
+        const int kind = p2g_record<DIM, T>(kp, g, in[u], org, rec, cell, status, fallbacks, base);
+        if (kind == kRecStray) p2g_scatter_record<DIM, T, Sink>(rec, base, g.R, sink);
+        if (kind != kRecTile) cell = -1;
 #pragma unroll
         for (int i = RF; i < RS; ++i) rec[i] = T(0);
         Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)lu * RS);
@@ -674,34 +749,71 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
       }
     }
     __syncthreads();
-    // phase 2: run heads (a particle whose cell differs from its predecessor's), compacted in
-    // order; runs[nruns] = chunk size, so run r spans [runs[r], runs[r + 1]).  Particles that failed
-    // the bounds check (cell -1) form runs of their own, skipped below.
+    // phase 2: group the chunk's particles by cell with a counting sort in shared memory (the
+    // chunk's order can come from a re-sort several substeps old, so equal cells need not be
+    // adjacent).  Run r is order[runs[r] .. runs[r + 1]): the particles of one cell.  Particles
+    // with cell -1 (outside the grid, or strays handled in phase 1) are left out.
     {
-      const int per_t = (ch.z + blockDim.x - 1) / blockDim.x;  // <= 2 for kChunk = 512
+      for (int c = threadIdx.x; c < ncell; c += blockDim.x) hist[c] = 0;
+      __syncthreads();
+      // one shared atomic per distinct cell of a warp (neighbouring particles mostly share a cell)
+      for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {
+        const int c = cells[l];
+        const unsigned act = __activemask();
+        const unsigned peers = __match_any_sync(act, c);
+        const int leader = __ffs(peers) - 1;
+        int first = 0;
+        if (c >= 0 && lane == leader) first = atomicAdd(&hist[c], __popc(peers));
+        first = __shfl_sync(peers, first, leader);
+        rank[l] = c >= 0 ? first + __popc(peers & lanemask_lt()) : -1;
+      }
+      __syncthreads();
+      const int per_t = (ncell + blockDim.x - 1) / blockDim.x;
       const int beg = threadIdx.x * per_t;
-      int heads = 0;
-      for (int l = beg; l < min(ch.z, beg + per_t); ++l) heads += (l == 0 || cells[l] != cells[l - 1]);
-      int inc = heads;
+      const int end = min(ncell, beg + per_t);
+      int cnt = 0, nz = 0;
+      for (int c = beg; c < end; ++c) {
+        cnt += hist[c];
+        nz += hist[c] > 0;
+      }
+      int icnt = cnt, inz = nz;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += t;
+        const int tc = __shfl_up_sync(0xffffffffu, icnt, o), tz = __shfl_up_sync(0xffffffffu, inz, o);
+        if (lane >= o) {
+          icnt += tc;
+          inz += tz;
+        }
       }
-      if (lane == 31) warp_cnt[warp] = inc;
+      if (lane == 31) {
+        warp_cnt[warp] = icnt;
+        warp_nz[warp] = inz;
+      }
       __syncthreads();
-      int before = 0, tot = 0;
+      int pos = 0, r = 0, tot_cnt = 0, tot_nz = 0;
 #pragma unroll
       for (int w = 0; w < kThreads / 32; ++w) {
-        before += w < warp ? warp_cnt[w] : 0;
-        tot += warp_cnt[w];
+        pos += w < warp ? warp_cnt[w] : 0;
+        r += w < warp ? warp_nz[w] : 0;
+        tot_cnt += warp_cnt[w];
+        tot_nz += warp_nz[w];
       }
-      int r = before + inc - heads;
-      for (int l = beg; l < min(ch.z, beg + per_t); ++l)
-        if (l == 0 || cells[l] != cells[l - 1]) runs[r++] = l;
+      pos += icnt - cnt;
+      r += inz - nz;
+      for (int c = beg; c < end; ++c) {
+        const int h = hist[c];
+        if (h > 0) runs[r++] = pos;
+        hist[c] = pos;  // start of cell c in order[]
+        pos += h;
+      }
       if (threadIdx.x == 0) {
-        nruns_s = tot;
-        runs[tot] = ch.z;
+        nruns_s = tot_nz;
+        runs[tot_nz] = tot_cnt;
+      }
+      __syncthreads();
+      for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {
+        const int c = cells[l];
+        if (c >= 0) order[hist[c] + rank[l]] = l;
       }
     }
     __syncthreads();
@@ -719,13 +831,12 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
     constexpr int w0 = RecLayout<DIM>::kW;
     for (int r = warp; r < nruns; r += kThreads / 32) {
       const int l0 = runs[r], l1 = runs[r + 1];
-      if (cells[l0] < 0) continue;
       T acc[3][4];
 #pragma unroll
       for (int i = 0; i < 3; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = T(0);
       if (active) {
-        for (int l = l0 + grp; l < l1; l += NG) {
-          const T* rc = recs + (size_t)l * RS;
+        for (int ll = l0 + grp; ll < l1; ll += NG) {
+          const T* rc = recs + (size_t)order[ll] * RS;
           T rv[RS];
           const Node4<T>* src = reinterpret_cast<const Node4<T>*>(rc);
 #pragma unroll
@@ -775,7 +886,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
           }
       }
       if (grp == 0) {
-        const int cl = cells[l0];
+        const int cl = cells[order[l0]];
         int lb[DIM];
         if constexpr (DIM == 3) {
           lb[2] = cl % g.bs;
@@ -870,7 +981,11 @@ __global__ void __launch_bounds__(kThreads) k_p2g_det(KParams<T> kp, Geom<DIM> g
           const int lu = u ? l2 : l;
           T rec[RS];
           int cell = -1;
-          if (!p2g_record<DIM, T>(kp, g, in[u], org, rec, cell, status, fallbacks)) cell = -1;
+          int base[DIM];
+          if (p2g_record<DIM, T>(kp, g, in[u], org, rec, cell, status, fallbacks, base) != kRecTile) {
+            if (cell < 0) raise_status(status, FFMPM_STATUS_OOB);  // a fresh plan has no strays
+            cell = -1;
+          }
 #pragma unroll
           for (int i = RF; i < RS; ++i) rec[i] = T(0);
           Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)lu * RS);
@@ -1241,6 +1356,11 @@ struct G2PExtra {
   uint32_t* keys_next;    // sorted mode: key of the updated position (next substep's sort input)
   uint32_t* block_count;  // sorted mode: histogram for the next substep
   int cell_bits;
+  // plans kept over several substeps: the global node grid for particles whose stencil left their
+  // chunk block's tile, and the flag raised when a particle's next stencil leaves the blocks within
+  // +-1 of that block (the next substep must then re-sort)
+  const void* grid_global;
+  uint32_t* far_flag;
 };
 
 // The state G2P reads of one particle (loaded ahead of the arithmetic so that the loads of
@@ -1268,25 +1388,33 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
                                              const G2PExtra& ex, const G2PIn<DIM, T>& in) {
   constexpr int DD = DIM * DIM;
   T xp[DIM], fx[DIM], w[3][DIM];
-  int lb[DIM];
-  bool ok = true;
+  int lb[DIM], base[DIM];
+  bool ok = true, in_tile = true;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     xp[d] = in.x[d];
-    int b;
-    ok = ok && base_of(xp[d], kp.inv_dx, kp.res, b, fx[d]);
-    lb[d] = b - org[d];
-    ok = ok && lb[d] >= 0 && lb[d] + 2 < g.tile;
+    ok = ok && base_of(xp[d], kp.inv_dx, kp.res, base[d], fx[d]);
+    lb[d] = base[d] - org[d];
+    in_tile = in_tile && lb[d] >= 0 && lb[d] + 2 < g.tile;
     T ww[3];
     bspline(fx[d], ww);
     w[0][d] = ww[0];
     w[1][d] = ww[1];
     w[2][d] = ww[2];
   }
-  if (!ok) {
+  if (!ok || (!in_tile && !ex.grid_global)) {
     raise_status(status, FFMPM_STATUS_OOB);
     return;
   }
+  // stencil source: the staged tile, or (a particle that left its chunk block's tile between
+  // re-sorts) the global node grid.  Node (i, j[, k]) of the stencil is src[i s0 + j s1 (+ k s2)]:
+  // 3D strides (W^2, W, 1), 2D strides (W, 1), W the row width of the source.
+  const int W = in_tile ? g.tile : g.R;
+  const int s0 = DIM == 3 ? W * W : W;
+  const int s1 = DIM == 3 ? W : 1;
+  const int s2 = 1;
+  const Node4<T>* src = in_tile ? tile + (DIM == 3 ? (lb[0] * W + lb[1]) * W + lb[2] : lb[0] * W + lb[1])
+                                : static_cast<const Node4<T>*>(ex.grid_global) + node_index<DIM>(g.R, base);
   // The gather runs on node velocities relative to the stencil's centre node u: v = u + sum w (v_i - u)
   // and C = 4 inv_dx sum w (v_i - u) (x) (i - fx), equal in exact arithmetic to the reference's
   // sums (the weights sum to 1 and sum w (i - fx) = 0).  A body's bulk velocity then cancels exactly
@@ -1297,10 +1425,9 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
   for (int d = 0; d < DIM; ++d) v[d] = T(0);
 #pragma unroll
   for (int i = 0; i < DD; ++i) Cn[i] = T(0);
-  const int T1 = g.tile;
   T u[DIM];
   if constexpr (DIM == 3) {
-    const Node4<T> c = tile[((lb[0] + 1) * T1 + (lb[1] + 1)) * T1 + (lb[2] + 1)];
+    const Node4<T> c = src[s0 + s1 + s2];
     u[0] = c.x;
     u[1] = c.y;
     u[2] = c.z;
@@ -1315,7 +1442,7 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
         for (int k = 0; k < 3; ++k) {
           const T d2 = T(k) - fx[2];
           const T weight = wij * w[k][2];
-          const Node4<T> gvn = tile[((lb[0] + i) * T1 + (lb[1] + j)) * T1 + (lb[2] + k)];
+          const Node4<T> gvn = src[i * s0 + j * s1 + k * s2];
           const T wv0 = weight * (gvn.x - u[0]), wv1 = weight * (gvn.y - u[1]), wv2 = weight * (gvn.z - u[2]);
           v[0] += wv0;
           v[1] += wv1;
@@ -1327,7 +1454,7 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
       }
     }
   } else {
-    const Node4<T> c = tile[(lb[0] + 1) * T1 + (lb[1] + 1)];
+    const Node4<T> c = src[s0 + s1];
     u[0] = c.x;
     u[1] = c.y;
 #pragma unroll
@@ -1337,7 +1464,7 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
       for (int j = 0; j < 3; ++j) {
         const T d1 = T(j) - fx[1];
         const T weight = w[i][0] * w[j][1];
-        const Node4<T> gvn = tile[(lb[0] + i) * T1 + (lb[1] + j)];
+        const Node4<T> gvn = src[i * s0 + j * s1];
         const T wv0 = weight * (gvn.x - u[0]), wv1 = weight * (gvn.y - u[1]);
         v[0] += wv0;
         v[1] += wv1;
@@ -1430,6 +1557,18 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
       if (!valid) raise_status(status, FFMPM_STATUS_OOB);
       ex.keys_next[q] = key;
       warp_count(ex.block_count, blk, valid);
+      if (ex.far_flag && valid) {
+        bool far = false;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          int bn;
+          T fn;
+          base_of(xn[d], kp.inv_dx, kp.res, bn, fn);
+          const int l = bn - org[d];
+          far = far || l < -g.bs || l > 2 * g.bs - 3;
+        }
+        if (far) *ex.far_flag = 1u;
+      }
     }
   }
 }
@@ -1438,7 +1577,9 @@ template <int DIM, typename T, bool kTma, bool kSorted>
 __global__ void __launch_bounds__(kThreads) k_g2p(KParams<T> kp, Geom<DIM> g, PView<T> Pin, PView<T> Pout,
                                                   const uint32_t* __restrict__ perm, const int4* __restrict__ chunks,
                                                   const WsHeader* __restrict__ hdr, const __grid_constant__ CUtensorMap tmap,
-                                                  const T* __restrict__ user_gv, G2PExtra ex, int32_t* status) {
+                                                  const T* __restrict__ user_gv, G2PExtra ex, int32_t* status,
+                                                  const uint32_t* __restrict__ sort_flag) {
+  if (sort_flag && *sort_flag == 0u) perm = nullptr;  // plan kept from an earlier substep: identity order
   // Dynamic shared memory: [pad to 128 B][tile: TN Node4][mbarrier].  The TMA destination must
   // be 128-byte aligned, so the tile start is rounded up explicitly.
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -1521,7 +1662,7 @@ __global__ void __launch_bounds__(kThreads) k_g2p(KParams<T> kp, Geom<DIM> g, PV
       const int l2 = l + blockDim.x;
       const bool two = l2 < ch.z;
       const uint32_t s1 = ch.y + l, s2 = ch.y + (two ? l2 : l);
-      const uint32_t p1 = perm[s1], p2 = perm[s2];
+      const uint32_t p1 = perm ? perm[s1] : s1, p2 = perm ? perm[s2] : s2;
       G2PIn<DIM, T> in1, in2;
       g2p_load<DIM, T>(Pin, p1, need_jp, in1);
       g2p_load<DIM, T>(Pin, p2, need_jp, in2);

@@ -35,7 +35,9 @@ constexpr uint32_t kLookbackSpins = 1u << 22;
 // Digit histograms of all passes (ghist[pass][256]), one read of the keys.  Nearly sorted keys put
 // equal digits in neighbouring lanes, so each warp first merges equal digits (__match_any_sync).
 __global__ void __launch_bounds__(kRsThreads) k_radix_ghist(const uint32_t* __restrict__ keys, uint32_t n,
-                                                             int passes, uint32_t* __restrict__ ghist) {
+                                                             int passes, uint32_t* __restrict__ ghist,
+                                                             const uint32_t* __restrict__ sort_flag) {
+  if (sort_flag && *sort_flag == 0u) return;
   __shared__ uint32_t h[kMaxRadixPasses][256];
   for (int i = threadIdx.x; i < kMaxRadixPasses * 256; i += kRsThreads) (&h[0][0])[i] = 0;
   __syncthreads();
@@ -77,7 +79,9 @@ __global__ void __launch_bounds__(kRsThreads) k_radix_onesweep(const uint32_t* _
                                                                 uint32_t* __restrict__ lookback,
                                                                 uint32_t* __restrict__ tile_counter,
                                                                 uint32_t* __restrict__ keys_out,
-                                                                uint32_t* __restrict__ vals_out, int32_t* status) {
+                                                                uint32_t* __restrict__ vals_out, int32_t* status,
+                                                                const uint32_t* __restrict__ sort_flag) {
+  if (sort_flag && *sort_flag == 0u) return;
   __shared__ uint32_t wcnt[kRsWarps][256];
   __shared__ uint32_t base[256];
   __shared__ uint32_t warp_sums[kRsWarps];
@@ -203,13 +207,13 @@ size_t radix_scratch_words(int passes, int64_t ntiles) {
 
 void radix_sort(const uint32_t* keys_in, uint32_t n, int passes, uint32_t* keys0, uint32_t* keys1, uint32_t* vals0,
                 uint32_t* vals1, uint32_t* scratch, int ntiles, int32_t* status, cudaStream_t s,
-                const uint32_t** keys_sorted, const uint32_t** perm) {
+                const uint32_t** keys_sorted, const uint32_t** perm, const uint32_t* sort_flag) {
   uint32_t* ghist = scratch;                    // [passes][256]
   uint32_t* counters = ghist + 256 * passes;    // [passes], 32-word padded
   uint32_t* lookback = counters + 32 * passes;  // [passes][ntiles][256]
   cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * radix_scratch_words(passes, ntiles), s);
   const int ghist_grid = std::max(1, std::min(ntiles, 2 * sm_count()));
-  k_radix_ghist<<<ghist_grid, kRsThreads, 0, s>>>(keys_in, n, passes, ghist);
+  k_radix_ghist<<<ghist_grid, kRsThreads, 0, s>>>(keys_in, n, passes, ghist, sort_flag);
   const uint32_t* kin = keys_in;
   const uint32_t* vin = nullptr;
   uint32_t* kbuf[2] = {keys0, keys1};
@@ -217,7 +221,7 @@ void radix_sort(const uint32_t* keys_in, uint32_t n, int passes, uint32_t* keys0
   for (int pass = 0; pass < passes; ++pass) {
     k_radix_onesweep<<<ntiles, kRsThreads, 0, s>>>(kin, vin, n, 8 * pass, ghist + 256 * pass,
                                                    lookback + (size_t)pass * ntiles * 256, counters + 32 * pass,
-                                                   kbuf[pass & 1], vbuf[pass & 1], status);
+                                                   kbuf[pass & 1], vbuf[pass & 1], status, sort_flag);
     kin = kbuf[pass & 1];
     vin = vbuf[pass & 1];
   }

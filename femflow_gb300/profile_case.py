@@ -26,12 +26,13 @@ def main():
     ap.add_argument("--dtype", choices=["f32", "f64"], default="f32")
     ap.add_argument("--variant", type=int, default=0, help="kernel variant flags (see ffmpm_params.variant)")
     ap.add_argument("--block-size", type=int, default=0)
+    ap.add_argument("--sort-every", type=int, default=8, help="substeps between re-sorts")
     args = ap.parse_args()
     s = two_cubes(args.n_per_cube)
     dtype = torch.float32 if args.dtype == "f32" else torch.float64
     solver = MPMSolver(torch.tensor(s["x"]), res=args.res, dt=args.dt, gravity=-9.8, volume=s["vol"],
                        mass=s["mass"], mu_0=s["mu"], lambda_0=s["lam"], v=torch.tensor(s["v"]), dtype=dtype,
-                       variant=args.variant, block_size=args.block_size)
+                       variant=args.variant, block_size=args.block_size, sort_every=args.sort_every)
     solver.step(args.warmup)
     torch.cuda.synchronize()
     t0 = time.perf_counter()

@@ -123,10 +123,10 @@ int ffmpm_substep(const ffmpm_params *p, ffmpm_particles *P, void *ws, size_t ws
 int ffmpm_substeps_sorted(const ffmpm_params *p, ffmpm_particles *a, ffmpm_particles *b, int32_t *ids_a,
                           int32_t *ids_b, int32_t nsteps, void *ws, size_t ws_bytes, void *stream);
 
-/* Stable radix sort of the particles by grid-block key (the key of each particle's base node):
- * keys_out[i] is the i-th smallest key, perm_out[i] the index of that particle.  Particles
- * outside the grid get key 0xFFFFFFFF and sort last.  No reference counterpart: it replaces the
- * reference's unordered particle loop (three_d/p2g.py:49). */
+/* Stable radix sort of the particles by grid-block key (the block of each particle's base node,
+ * then its cell inside the block): keys_out[i] is the i-th smallest key, perm_out[i] the index of
+ * that particle.  Particles outside the grid get key 0xFFFFFFFF and sort last.  No reference
+ * counterpart: it replaces the reference's unordered particle loop (three_d/p2g.py:49). */
 int ffmpm_sort_by_block(const ffmpm_params *p, const void *x, int64_t n, uint32_t *keys_out, uint32_t *perm_out,
                         void *ws, size_t ws_bytes, void *stream);
 

@@ -66,14 +66,14 @@ def _scene(dtype, n_per=3000, res=32):
     return s
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant,sort_every", [(0, 1), (1, 1), (2, 1), (0, 3), (0, 8)])
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
-def test_sorted_solver_matches_in_place_substeps(dtype, variant):
+def test_sorted_solver_matches_in_place_substeps(dtype, variant, sort_every):
     s = _scene(dtype)
     res, dt, g, steps = s["res"], 2e-4, -9.8, 10
     solver = MPMSolver(torch.tensor(s["x"]), res=res, dt=dt, gravity=g, volume=s["vol"],
                        mass=torch.tensor(s["mass"]), mu_0=torch.tensor(s["mu"]), lambda_0=torch.tensor(s["lam"]),
-                       v=torch.tensor(s["v"]), dtype=dtype, variant=variant)
+                       v=torch.tensor(s["v"]), dtype=dtype, variant=variant, sort_every=sort_every)
     solver.step(steps, check=True)
     got = solver.state()
     N_ = len(s["x"])
@@ -89,6 +89,35 @@ def test_sorted_solver_matches_in_place_substeps(dtype, variant):
     # the ids are a permutation and the state stays sorted by block
     ids = solver.sorted_state()["ids"].cpu().numpy()
     assert np.array_equal(np.sort(ids), np.arange(N_))
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_fast_particles_between_sorts(dtype):
+    """A cube crossing several blocks between scheduled re-sorts (25 substeps apart): particles whose
+    stencil leaves their block's tile take the direct paths, and particles that leave the blocks
+    around it trigger an early re-sort; the result equals the in-place substeps."""
+    rng = np.random.default_rng(5)
+    n_, res, dt, g, steps = 6000, 64, 2e-4, -9.8, 40
+    x = rng.uniform(-0.08, 0.08, (n_, 3)) + 0.5
+    v = np.tile([[30.0, -20.0, 15.0]], (n_, 1)) + rng.normal(0, 0.5, (n_, 3))  # ~0.4 cells per substep
+    vol = 0.16 ** 3 / n_
+    E_, nu = 2e3, 0.3
+    mu, lam = E_ / (2 * (1 + nu)), E_ * nu / ((1 + nu) * (1 - 2 * nu))
+    solver = MPMSolver(torch.tensor(x), res=res, dt=dt, gravity=g, volume=vol, mass=vol, mu_0=mu, lambda_0=lam,
+                       v=torch.tensor(v), dtype=dtype, sort_every=25)
+    solver.step(steps, check=True)
+    got = solver.state()
+    ps = ParticleSet(t(x, dtype), t(np.full(n_, vol), dtype), t(np.full(n_, mu), dtype), t(np.full(n_, lam), dtype))
+    vv, F, C, Jp = mls_mpm.make_mls_mpm_coefficients(n_, 3, dtype=dtype)
+    vv.copy_(t(v, dtype))
+    for _ in range(steps):
+        mls_mpm.solve_mls_mpm_3d(res, float(res), 1.0, 1 / res, dt, vol, g, ps, vv, F, C, Jp)
+    rel = 1e-12 if dtype == torch.float64 else 1e-5
+    close(n(got["x"]), n(ps.pos), rel, scale=1.0, what="x")
+    close(n(got["v"]), n(vv), 50 * rel, scale=float(np.abs(v).max()), what="v")
+    close(n(got["F"]), n(F), 10 * rel, scale=1.0, what="F")
+    moved = np.abs(n(got["x"]) - x).max()
+    assert moved * res > 12  # more than a block of 8 cells, ~10 cells between scheduled re-sorts
 
 
 def test_graph_replay_matches_direct_launches():
