@@ -137,6 +137,7 @@ def run_ours(args):
     import torch.distributed as dist
 
     from femflow_gb300 import engine as E
+    from femflow_gb300 import replicas as REP
     from femflow_gb300.solver import MPMSolver
     from femflow_gb300.solvers.mpm import mls_mpm, three_d
     from femflow_gb300.solvers.mpm.particle import ParticleSet
@@ -149,9 +150,7 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl", device_id=dev)
 
-    def barrier():
-        if world > 1:
-            dist.barrier()
+    barrier = REP.barrier
 
     s = scene()
     n = s["n"]
@@ -181,11 +180,7 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     t_wall1 = time.time()
     barrier()
-    t = ev0.elapsed_time(ev1) / 1e3
-    if world > 1:
-        tt = torch.tensor([t], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
+    t = REP.max_over_ranks(ev0.elapsed_time(ev1) / 1e3, dev)
     status, fallbacks = solver.status()
     clocks.stop()
     value = world * n * args.steps / t
@@ -239,11 +234,7 @@ def run_ours(args):
     for _ in range(e2e_steps):
         mls_mpm.solve_mls_mpm_3d(RES, float(RES), 1.0, 1 / RES, DT, s["vol"], GRAVITY, pset, v_h, F_h, C_h, J_h)
     torch.cuda.synchronize(dev)
-    te = time.perf_counter() - e0
-    if world > 1:
-        tt = torch.tensor([te], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        te = float(tt.item())
+    te = REP.max_over_ranks(time.perf_counter() - e0, dev)
     out["e2e"] = {"value": world * n * e2e_steps / te, "unit": UNIT, "h2d_bytes_per_step": n * (12 + 12 + 12 + 36 + 36 + 4),
                   "d2h_bytes_per_step": n * (12 + 12 + 36 + 36 + 4), "steps": e2e_steps,
                   "api": "solve_mls_mpm_3d on pinned host float32 arrays (staged H2D, substep, written back D2H)"}

@@ -150,3 +150,78 @@ def random_scenes(nscenes: int = 256, seed: int = 0, n_range=(2048, 65536), res_
         mu, lam = E / (2 * (1 + nu)), E * nu / ((1 + nu) * (1 - 2 * nu))
         out.append(dict(x=x, res=res, dt=dt, mass=vol, volume=vol, mu_0=mu, lambda_0=lam, E=E, nu=nu))
     return out
+
+
+def stable_variant(scenes: List[Dict], cfl: float = 0.5) -> List[Dict]:
+    """The same scenes with E capped so that the elastic wave crosses at most `cfl` cells per
+    substep (c = sqrt((lam + 2 mu) / rho), rho = mass / volume)."""
+    out = []
+    for s in scenes:
+        s = dict(s)
+        E, nu = s["E"], s["nu"]
+        rho = s["mass"] / s["volume"]
+        k = (1 - nu) / ((1 + nu) * (1 - 2 * nu))  # (lam + 2 mu) / E
+        E_max = rho * (cfl / (s["dt"] * s["res"])) ** 2 / k
+        if E > E_max:
+            E = E_max
+            s["E"] = E
+            s["mu_0"], s["lambda_0"] = E / (2 * (1 + nu)), E * nu / ((1 + nu) * (1 - 2 * nu))
+        out.append(s)
+    return out
+
+
+def measure(scenes: List[Dict], steps: int = 100, reps: int = 3, sequential: bool = True) -> dict:
+    """Particle-substeps/s of the batch (autotuned launch shape, `steps`-substep CUDA graph) and,
+    for comparison, of the same scenes stepped one at a time on the resident single-scene solver."""
+    from .solver import MPMSolver
+
+    b = Batch2D(scenes)
+    best, timings = b.autotune()
+    b.capture(steps)
+    b.step(steps)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.step(steps * reps)
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    out = dict(scenes=len(scenes), particles=b.n, substeps=steps * reps, graph_substeps=steps,
+               launch_shape=dict(threads=best[0], ctas_per_sm=best[1]),
+               autotune_ms={f"{k[0]}x{k[1]}": v for k, v in timings.items()},
+               batched=dict(seconds=t, particle_substeps_per_s=b.n * steps * reps / t), status=b.status())
+    if sequential:
+        solvers = [MPMSolver(torch.tensor(s["x"]), res=s["res"], dt=s["dt"], gravity=-9.8, volume=s["volume"],
+                             mass=s["mass"], mu_0=s["mu_0"], lambda_0=s["lambda_0"], dtype=torch.float32)
+                   for s in scenes]
+        for sv in solvers:
+            sv.step(2)
+        torch.cuda.synchronize()
+        e0.record()
+        for sv in solvers:
+            sv.step(steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ts = e0.elapsed_time(e1) / 1e3
+        out["one_scene_at_a_time"] = dict(seconds=ts, particle_substeps_per_s=b.n * steps / ts)
+        out["speedup_batched"] = out["batched"]["particle_substeps_per_s"] / out["one_scene_at_a_time"][
+            "particle_substeps_per_s"]
+    return out
+
+
+def main(argv=None):
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="throughput of the batched 2D scenes")
+    ap.add_argument("--scenes", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--seed", type=int, default=0)
+    a = ap.parse_args(argv)
+    sc = random_scenes(a.scenes, seed=a.seed)
+    rep = {"as_written": measure(sc, a.steps, sequential=False), "stable_variant": measure(stable_variant(sc), a.steps)}
+    print(json.dumps(rep, indent=1, default=float))
+
+
+if __name__ == "__main__":
+    main()

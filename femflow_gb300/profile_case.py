@@ -27,12 +27,14 @@ def main():
     ap.add_argument("--variant", type=int, default=0, help="kernel variant flags (see ffmpm_params.variant)")
     ap.add_argument("--block-size", type=int, default=0)
     ap.add_argument("--sort-every", type=int, default=8, help="substeps between re-sorts")
+    ap.add_argument("--deterministic", action="store_true", help="bit-reproducible P2G (re-sorts every substep)")
     args = ap.parse_args()
     s = two_cubes(args.n_per_cube)
     dtype = torch.float32 if args.dtype == "f32" else torch.float64
     solver = MPMSolver(torch.tensor(s["x"]), res=args.res, dt=args.dt, gravity=-9.8, volume=s["vol"],
                        mass=s["mass"], mu_0=s["mu"], lambda_0=s["lam"], v=torch.tensor(s["v"]), dtype=dtype,
-                       variant=args.variant, block_size=args.block_size, sort_every=args.sort_every)
+                       variant=args.variant, block_size=args.block_size, sort_every=args.sort_every,
+                       deterministic=args.deterministic)
     solver.step(args.warmup)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
