@@ -423,18 +423,27 @@ __device__ __forceinline__ void lame_of(const KParams<T>& kp, const PView<T>& P,
   lam = lam0 * e;
 }
 
+// Shared-memory float add whose result is not needed: a reduction (red), not a read-modify-write
+// that returns the old value.
+__device__ __forceinline__ void smem_add(float* p, float v) {
+  asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(p))), "f"(v)
+               : "memory");
+}
+__device__ __forceinline__ void smem_add(double* p, double v) { atomicAdd(p, v); }
+
 // Accumulation targets of one particle's 3^DIM contributions, addressed by node coordinates
 // relative to the block origin.
+
 template <int DIM, typename T>
 struct TileAdder {  // shared tile, SoA: 4 arrays of TN values
   T* tile;
   int TN, T1;
   __device__ __forceinline__ void add(int li, int lj, int lk, T a, T b, T c, T m) const {
     const int idx = DIM == 3 ? (li * T1 + lj) * T1 + lk : li * T1 + lj;
-    atomicAdd(&tile[idx], a);
-    atomicAdd(&tile[TN + idx], b);
-    if constexpr (DIM == 3) atomicAdd(&tile[2 * TN + idx], c);
-    atomicAdd(&tile[3 * TN + idx], m);
+    smem_add(&tile[idx], a);
+    smem_add(&tile[TN + idx], b);
+    if constexpr (DIM == 3) smem_add(&tile[2 * TN + idx], c);
+    smem_add(&tile[3 * TN + idx], m);
   }
 };
 
@@ -651,12 +660,16 @@ __device__ __forceinline__ int p2g_record(const KParams<T>& kp, const Geom<DIM>&
   return in_tile ? kRecTile : kRecStray;
 }
 
-// Scatter one record straight to the global grid through the sink (a particle whose stencil left
-// its chunk block's tile): node (i, j[, k]) gets w (q + dx A (i, j[, k])) and w m.
+// Scatter one record (in shared memory) straight to the global grid through the sink: a particle
+// whose stencil left its chunk block's tile.  Its base node is in the record's padding,
+// rec[kFloats + d] (exact: node indices are far below 2^24).  Node (i, j[, k]) gets
+// w (q + dx A (i, j[, k])) and w m.
 template <int DIM, typename T, typename Sink>
-__device__ __noinline__ void p2g_scatter_record(const T* rec, const int base[DIM], int R, const Sink& sink) {
+__device__ void p2g_scatter_record(const T* rec, int R, const Sink& sink) {
   constexpr int a0 = 1 + DIM;
   constexpr int w0 = RecLayout<DIM>::kW;
+  int base[DIM];
+  for (int d = 0; d < DIM; ++d) base[d] = static_cast<int>(rec[RecLayout<DIM>::kFloats + d]);
   const T m = rec[0];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j)
@@ -738,10 +751,16 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
         T rec[RS];
         int cell = -1, base[DIM];
         const int kind = p2g_record<DIM, T>(kp, g, in[u], org, rec, cell, status, fallbacks, base);
-        if (kind == kRecStray) p2g_scatter_record<DIM, T, Sink>(rec, base, g.R, sink);
-        if (kind != kRecTile) cell = -1;
 #pragma unroll
         for (int i = RF; i < RS; ++i) rec[i] = T(0);
+        if (kind == kRecStray) {
+          // scattered after the phase (below); its base node rides in the record's padding
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) rec[RF + d] = T(base[d]);
+          cell = -2;
+        } else if (kind != kRecTile) {
+          cell = -1;
+        }
         Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)lu * RS);
 #pragma unroll
         for (int i = 0; i < RS / 4; ++i) dst[i] = Node4<T>{rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]};
@@ -749,6 +768,9 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
       }
     }
     __syncthreads();
+    // particles whose stencil left the block's tile (only between re-sorts): direct global adds
+    for (int l = threadIdx.x; l < ch.z; l += blockDim.x)
+      if (cells[l] == -2) p2g_scatter_record<DIM, T, Sink>(recs + (size_t)l * RS, g.R, sink);
     // phase 2: group the chunk's particles by cell with a counting sort in shared memory (the
     // chunk's order can come from a re-sort several substeps old, so equal cells need not be
     // adjacent).  Run r is order[runs[r] .. runs[r + 1]): the particles of one cell.  Particles
@@ -835,18 +857,21 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
 #pragma unroll
       for (int i = 0; i < 3; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = T(0);
       if (active) {
-        for (int ll = l0 + grp; ll < l1; ll += NG) {
-          const T* rc = recs + (size_t)order[ll] * RS;
-          T rv[RS];
-          const Node4<T>* src = reinterpret_cast<const Node4<T>*>(rc);
+        // RU floats of a record are used (the rest is padding); two records per step, both loaded
+        // before either is accumulated, so that shared-memory latency overlaps
+        constexpr int RU = (RecLayout<DIM>::kFloats + 3) / 4 * 4;
+        auto load = [&](int ll, T (&rv)[RU]) {
+          const Node4<T>* src = reinterpret_cast<const Node4<T>*>(recs + (size_t)order[ll] * RS);
 #pragma unroll
-          for (int i = 0; i < RS / 4; ++i) {
+          for (int i = 0; i < RU / 4; ++i) {
             const Node4<T> q4 = src[i];
             rv[4 * i] = q4.x;
             rv[4 * i + 1] = q4.y;
             rv[4 * i + 2] = q4.z;
             rv[4 * i + 3] = q4.w;
           }
+        };
+        auto accum = [&](const T (&rv)[RU]) {
           const T m = rv[0];
           T wjk;
           if constexpr (DIM == 3) {
@@ -872,6 +897,19 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
             for (int rr = 0; rr < DIM; ++rr) acc[i][rr] += wgt * (base[rr] + T(i) * step[rr]);
             acc[i][3] += wgt * m;
           }
+        };
+        int ll = l0 + grp;
+        for (; ll + NG < l1; ll += 2 * NG) {
+          T ra[RU], rb[RU];
+          load(ll, ra);
+          load(ll + NG, rb);
+          accum(ra);
+          accum(rb);
+        }
+        if (ll < l1) {
+          T ra[RU];
+          load(ll, ra);
+          accum(ra);
         }
       }
       // fold the NG groups onto group 0 (lanes 0..LP-1)
