@@ -186,18 +186,22 @@ __device__ __forceinline__ int polar3_newton(const T F[9], T R[9], int max_iter,
 // Polar factor used by the stress.  In float, F whose smallest singular value is small relative
 // to its largest (|det F| / (|F|_F/sqrt 3)^3 at most 1e-3) or where the float iteration does not
 // settle is redone in double; `fallbacks` counts those particles.
+// The double redo of a float polar factor: a call of its own (rarely taken), so that its double
+// registers do not count against the float kernels that inline polar3.
+static __device__ __noinline__ void polar3_redo_fp64(const float* F, float* R, uint32_t* fallbacks) {
+  double Fd[9], Rd[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) Fd[i] = double(F[i]);
+  polar3_newton(Fd, Rd, 60);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) R[i] = float(Rd[i]);
+  if (fallbacks) atomicAdd(fallbacks, 1u);
+}
+
 template <typename T>
 __device__ __forceinline__ void polar3(const T F[9], T R[9], uint32_t* fallbacks) {
   if constexpr (sizeof(T) == 4) {
-    if (polar3_newton(F, R, 12, T(1e-3)) < 0) {
-      double Fd[9], Rd[9];
-#pragma unroll
-      for (int i = 0; i < 9; ++i) Fd[i] = double(F[i]);
-      polar3_newton(Fd, Rd, 60);
-#pragma unroll
-      for (int i = 0; i < 9; ++i) R[i] = T(Rd[i]);
-      if (fallbacks) atomicAdd(fallbacks, 1u);
-    }
+    if (polar3_newton(F, R, 12, T(1e-3)) < 0) polar3_redo_fp64(F, R, fallbacks);
   } else {
     // double: a failure means F is singular to working precision; the last iterate is kept (the
     // reference's LAPACK answer is arbitrary in the null space there) and counted.

@@ -734,38 +734,30 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
 #pragma unroll
       for (int d = 0; d < DIM; ++d) org[d] = bc[d] * g.bs;
     }
-    // phase 1: one record per particle (cell -1 marks a particle that failed the bounds check).
-    // Two particles per thread per iteration, both loaded before either is computed.
-    for (int l = threadIdx.x; l < ch.z; l += 2 * blockDim.x) {
-      const int l2 = l + blockDim.x;
-      const bool two = l2 < ch.z;
-      const uint32_t s1 = ch.y + l, s2 = ch.y + (two ? l2 : l);
-      const uint32_t p1 = perm ? perm[s1] : s1, p2 = perm ? perm[s2] : s2;
-      P2GIn<DIM, T> in[2];
-      p2g_load<DIM, T>(kp, P, p1, in[0]);
-      p2g_load<DIM, T>(kp, P, p2, in[1]);
+    // phase 1: one record per particle and thread (cell -1 marks a particle that failed the bounds
+    // check, -2 one whose stencil left the block's tile).  One particle at a time: two in flight per
+    // thread cost more registers than their overlapped loads gain.
+    for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {
+      const uint32_t s = ch.y + l;
+      P2GIn<DIM, T> in;
+      p2g_load<DIM, T>(kp, P, perm ? perm[s] : s, in);
+      T rec[RS];
+      int cell = -1, base[DIM];
+      const int kind = p2g_record<DIM, T>(kp, g, in, org, rec, cell, status, fallbacks, base);
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        if (u == 1 && !two) break;
-        const int lu = u ? l2 : l;
-        T rec[RS];
-        int cell = -1, base[DIM];
-        const int kind = p2g_record<DIM, T>(kp, g, in[u], org, rec, cell, status, fallbacks, base);
+      for (int i = RF; i < RS; ++i) rec[i] = T(0);
+      if (kind == kRecStray) {
+        // scattered after the phase (below); its base node rides in the record's padding
 #pragma unroll
-        for (int i = RF; i < RS; ++i) rec[i] = T(0);
-        if (kind == kRecStray) {
-          // scattered after the phase (below); its base node rides in the record's padding
-#pragma unroll
-          for (int d = 0; d < DIM; ++d) rec[RF + d] = T(base[d]);
-          cell = -2;
-        } else if (kind != kRecTile) {
-          cell = -1;
-        }
-        Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)lu * RS);
-#pragma unroll
-        for (int i = 0; i < RS / 4; ++i) dst[i] = Node4<T>{rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]};
-        cells[lu] = cell;
+        for (int d = 0; d < DIM; ++d) rec[RF + d] = T(base[d]);
+        cell = -2;
+      } else if (kind != kRecTile) {
+        cell = -1;
       }
+      Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)l * RS);
+#pragma unroll
+      for (int i = 0; i < RS / 4; ++i) dst[i] = Node4<T>{rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]};
+      cells[l] = cell;
     }
     __syncthreads();
     // particles whose stencil left the block's tile (only between re-sorts): direct global adds
@@ -857,30 +849,33 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
 #pragma unroll
       for (int i = 0; i < 3; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = T(0);
       if (active) {
-        // RU floats of a record are used (the rest is padding); two records per step, both loaded
-        // before either is accumulated, so that shared-memory latency overlaps
-        constexpr int RU = (RecLayout<DIM>::kFloats + 3) / 4 * 4;
-        auto load = [&](int ll, T (&rv)[RU]) {
-          const Node4<T>* src = reinterpret_cast<const Node4<T>*>(recs + (size_t)order[ll] * RS);
+        // a lane needs m, q, dx A and the x weights (the first RU floats: whole float4s) and its own
+        // y (and z) weight; two records per step, both loaded before either is accumulated
+        constexpr int RU = DIM == 3 ? 16 : 12;
+        struct Rv {
+          T v[RU];
+          T wjk;
+        };
+        auto load = [&](int ll, Rv& rv) {
+          const T* rc = recs + (size_t)order[ll] * RS;
+          const Node4<T>* src = reinterpret_cast<const Node4<T>*>(rc);
 #pragma unroll
           for (int i = 0; i < RU / 4; ++i) {
             const Node4<T> q4 = src[i];
-            rv[4 * i] = q4.x;
-            rv[4 * i + 1] = q4.y;
-            rv[4 * i + 2] = q4.z;
-            rv[4 * i + 3] = q4.w;
+            rv.v[4 * i] = q4.x;
+            rv.v[4 * i + 1] = q4.y;
+            rv.v[4 * i + 2] = q4.z;
+            rv.v[4 * i + 3] = q4.w;
           }
+          if constexpr (DIM == 3)
+            rv.wjk = rc[w0 + 3 + oj] * rc[w0 + 6 + ok];
+          else
+            rv.wjk = rc[w0 + 3 + oj];
         };
-        auto accum = [&](const T (&rv)[RU]) {
+        auto accum = [&](const Rv& r) {
+          const T* rv = r.v;
           const T m = rv[0];
-          T wjk;
-          if constexpr (DIM == 3) {
-            const T wy = oj == 0 ? rv[w0 + 3] : (oj == 1 ? rv[w0 + 4] : rv[w0 + 5]);
-            const T wz = ok == 0 ? rv[w0 + 6] : (ok == 1 ? rv[w0 + 7] : rv[w0 + 8]);
-            wjk = wy * wz;
-          } else {
-            wjk = oj == 0 ? rv[w0 + 3] : (oj == 1 ? rv[w0 + 4] : rv[w0 + 5]);
-          }
+          const T wjk = r.wjk;
           // base_r = q_r + a_r1 j (+ a_r2 k); node i adds i * a_r0
           T base[DIM], step[DIM];
 #pragma unroll
@@ -900,14 +895,14 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
         };
         int ll = l0 + grp;
         for (; ll + NG < l1; ll += 2 * NG) {
-          T ra[RU], rb[RU];
+          Rv ra, rb;
           load(ll, ra);
           load(ll + NG, rb);
           accum(ra);
           accum(rb);
         }
         if (ll < l1) {
-          T ra[RU];
+          Rv ra;
           load(ll, ra);
           accum(ra);
         }
@@ -1469,26 +1464,44 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
     u[0] = c.x;
     u[1] = c.y;
     u[2] = c.z;
+    // The weights are separable, w = wx_i wy_j wz_k, so the 27-node sums are taken one axis at a
+    // time: along k for each (i, j) (the sums s0 = sum_k wz_k g and s1 = sum_k wz_k (k - fz) g),
+    // then along j, then along i; 360 multiply-adds where the node-by-node form takes 513.
+    T wzd[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) wzd[k] = w[k][2] * (T(k) - fx[2]);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      const T d0 = T(i) - fx[0];
+      T t0[3] = {T(0), T(0), T(0)}, t1[3] = {T(0), T(0), T(0)}, t2[3] = {T(0), T(0), T(0)};
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        const T d1 = T(j) - fx[1];
-        const T wij = w[i][0] * w[j][1];
+        T sa[3] = {T(0), T(0), T(0)}, sb[3] = {T(0), T(0), T(0)};
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          const T d2 = T(k) - fx[2];
-          const T weight = wij * w[k][2];
           const Node4<T> gvn = src[i * s0 + j * s1 + k * s2];
-          const T wv0 = weight * (gvn.x - u[0]), wv1 = weight * (gvn.y - u[1]), wv2 = weight * (gvn.z - u[2]);
-          v[0] += wv0;
-          v[1] += wv1;
-          v[2] += wv2;
-          Cn[0] += wv0 * d0; Cn[1] += wv0 * d1; Cn[2] += wv0 * d2;
-          Cn[3] += wv1 * d0; Cn[4] += wv1 * d1; Cn[5] += wv1 * d2;
-          Cn[6] += wv2 * d0; Cn[7] += wv2 * d1; Cn[8] += wv2 * d2;
+          const T g0 = gvn.x - u[0], g1 = gvn.y - u[1], g2 = gvn.z - u[2];
+          sa[0] += w[k][2] * g0;
+          sa[1] += w[k][2] * g1;
+          sa[2] += w[k][2] * g2;
+          sb[0] += wzd[k] * g0;
+          sb[1] += wzd[k] * g1;
+          sb[2] += wzd[k] * g2;
         }
+        const T wy = w[j][1], wyd = w[j][1] * (T(j) - fx[1]);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          t0[r] += wy * sa[r];
+          t1[r] += wyd * sa[r];
+          t2[r] += wy * sb[r];
+        }
+      }
+      const T wx = w[i][0], wxd = w[i][0] * (T(i) - fx[0]);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        v[r] += wx * t0[r];
+        Cn[r * 3 + 0] += wxd * t0[r];
+        Cn[r * 3 + 1] += wx * t1[r];
+        Cn[r * 3 + 2] += wx * t2[r];
       }
     }
   } else {
