@@ -30,8 +30,8 @@ STATUS_NONFINITE = 2
 STATUS_TIMEOUT = 4
 
 MODELS = {"neo_hookean": 0, "snow": 1, "fixed_corotated": 2}
-NPHASES = 6
-PHASES = ("keys", "sort", "plan", "p2g", "grid_update", "g2p")
+NPHASES = 7
+PHASES = ("keys", "sort", "plan", "p2g", "grid_update", "g2p", "g2p2g")
 WALLS = {"reference": 0, "sticky3": 1}
 
 
@@ -97,6 +97,7 @@ _PROTOS = {
     "ffmpm_profile_substeps": (ctypes.c_int, [_P(Params), _P(Particles), _P(Particles), _vp, _vp, ctypes.c_int32,
                                               _vp, ctypes.c_size_t, _vp, _P(ctypes.c_double), _P(ctypes.c_int64)]),
     "ffmpm_plan_info": (ctypes.c_int, [_P(Params), ctypes.c_int64, _P(ctypes.c_int64)]),
+    "ffmpm_kernels_per_call": (ctypes.c_int, [_P(Params), ctypes.c_int64, ctypes.c_int32, _P(ctypes.c_int64)]),
     "ffmpm_sort_by_block_static": (ctypes.c_int, [_P(Params), _vp, ctypes.c_int64, _vp, _vp, _vp]),
     "ffmpm_batch2d_workspace_size": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32, _P(ctypes.c_size_t)]),
     "ffmpm_batch2d_init": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_size_t, _vp]),

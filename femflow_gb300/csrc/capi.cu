@@ -58,7 +58,6 @@ bool make_layout(const ffmpm_params& p, int64_t n, Layout* L) {
   L->tile = L->bs + 2;
   L->nblocks = p.dim == 3 ? int64_t(L->nb) * L->nb * L->nb : int64_t(L->nb) * L->nb;
   L->nnodes = p.dim == 3 ? int64_t(L->R) * L->R * L->R : int64_t(L->R) * L->R;
-  // keys order particles by block, then by cell inside the block
   // keys order particles by block, then by cell inside the block, so that each P2G chunk spans few
   // cells (between re-sorts the P2G regroups each chunk by cell itself)
   L->cell_bits = p.dim * ilog2_ceil(L->bs);
@@ -82,6 +81,7 @@ bool make_layout(const ffmpm_params& p, int64_t n, Layout* L) {
   L->off_block_cnt = take(sizeof(uint32_t) * L->nblocks);
   L->off_chunks = take(sizeof(int4) * L->max_chunks);
   L->off_touched = take(sizeof(uint32_t) * L->nblocks);
+  L->off_tmark = take(sizeof(uint32_t) * L->nblocks);
   L->off_occupied = take(sizeof(int4) * L->nblocks);
   L->off_keys_next = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
   L->off_keys0 = take(sizeof(uint32_t) * std::max<int64_t>(n, 1));
@@ -155,7 +155,7 @@ Geom<DIM> geom(const Layout& L) {
 struct Ws {
   unsigned char* base;
   WsHeader* hdr;
-  uint32_t *block_count, *block_start, *block_cnt, *touched, *keys_next, *keys0, *keys1, *vals0, *vals1, *hist;
+  uint32_t *block_count, *block_start, *block_cnt, *touched, *tmark, *keys_next, *keys0, *keys1, *vals0, *vals1, *hist;
   int4 *chunks, *occupied;
   void *gridA, *gridB, *stage;
 };
@@ -169,6 +169,7 @@ Ws bind(void* ws, const Layout& L) {
   w.block_cnt = reinterpret_cast<uint32_t*>(w.base + L.off_block_cnt);
   w.chunks = reinterpret_cast<int4*>(w.base + L.off_chunks);
   w.touched = reinterpret_cast<uint32_t*>(w.base + L.off_touched);
+  w.tmark = reinterpret_cast<uint32_t*>(w.base + L.off_tmark);
   w.occupied = reinterpret_cast<int4*>(w.base + L.off_occupied);
   w.keys_next = reinterpret_cast<uint32_t*>(w.base + L.off_keys_next);
   w.keys0 = reinterpret_cast<uint32_t*>(w.base + L.off_keys0);
@@ -275,8 +276,8 @@ void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const PV
              &ks, perm, flag);
   if (tm) tm->end(1 + L.passes);
   if (tm) tm->begin(2);
-  k_plan<DIM><<<1, 1024, 0, s>>>(g, w.block_count, w.block_start, w.block_cnt, w.chunks, w.touched, w.occupied,
-                                 w.hdr, flag, flag ? 1 : 0);
+  k_plan<DIM><<<1, 1024, 0, s>>>(g, w.block_count, w.block_start, w.block_cnt, w.chunks, w.touched, w.tmark,
+                                 w.occupied, w.hdr, flag, flag ? 1 : 0);
   if (tm) tm->end(1);
 }
 
@@ -306,9 +307,7 @@ void launch_p2g(const ffmpm_params& p, const Layout& L, const Ws& w, const PView
   const bool lanes = !flag && (p.variant & kVariantP2GLanes) != 0;
   if (!direct && !lanes) {
     // default: cell-run P2G (tile + per-particle records + cell ids + run starts)
-    const int ncell = DIM == 3 ? L.bs * L.bs * L.bs : L.bs * L.bs;
-    const size_t smem = tile_smem<DIM, T>(L) + size_t(kChunk) * RecLayout<DIM>::kStride * sizeof(T) +
-                        sizeof(int) * (3 * kChunk + std::max(kChunk, ncell) + 1 + ncell);
+    const size_t smem = tile_smem<DIM, T>(L) + cell_run_smem_bytes<DIM, T>(L.bs);
     auto kern = k_p2g_cells<DIM, T, Sink>;
     set_smem(kern, smem);
     kern<<<work_grid(L.max_chunks, resident_per_sm(kern, smem)), kThreads, smem, s>>>(
@@ -363,6 +362,29 @@ int launch_g2p(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<
   return FFMPM_OK;
 }
 
+template <int DIM, typename T>
+int launch_g2p2g(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<T>& Pin, const PView<T>& Pout,
+                 const uint32_t* perm, const G2PExtra& ex, cudaStream_t s, const uint32_t* flag) {
+  alignas(64) CUtensorMap map;
+  std::memset(&map, 0, sizeof(map));
+  if (!encode_grid_map(&map, w.gridB, L)) return FFMPM_ERR_CUDA;
+  const int tn = DIM == 3 ? L.tile * L.tile * L.tile : L.tile * L.tile;
+  const size_t smem = g2p2g_smem_bytes<DIM, T>(tn, L.bs);
+  auto kern = k_g2p2g<DIM, T>;
+  set_smem(kern, smem);
+  kern<<<work_grid(L.max_chunks, resident_per_sm(kern, smem)), kThreads, smem, s>>>(
+      kparams<T>(p), geom<DIM>(L), Pin, Pout, perm, w.chunks, w.hdr, map, ex,
+      InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, w.tmark, w.touched, &w.hdr->status, &w.hdr->polar_fallbacks,
+      flag);
+  return FFMPM_OK;
+}
+
+// Fused G2P + P2G in the sorted solver: the default outside the deterministic mode and the P2G
+// variants, for runs of two or more substeps.
+bool fused(const ffmpm_params& p, int nsteps) {
+  return !p.deterministic && nsteps >= 2 && (p.variant & (kVariantNoFuse | kVariantP2GDirect | kVariantP2GLanes)) == 0;
+}
+
 // ------------------------------------------------------------------------------------ operations
 template <int DIM, typename T>
 int op_substep(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_particles* P, cudaStream_t s) {
@@ -381,10 +403,59 @@ int op_substep(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_partic
   return rc != FFMPM_OK ? rc : check_launch();
 }
 
+// Substeps 0..n-1 with the fused kernel: P2G(0), then for k = 0..n-2: grid update(k), re-sort if
+// due, G2P(k) + P2G(k+1); then grid update(n-1) and G2P(n-1).  The state after every substep is
+// in buffer a or b as in the unfused loop (x, F, Jp, ids, per-particle material), with v and C
+// written by the last G2P only.  The grid update of substep k runs before the re-sort, on the
+// touched blocks of the plan its P2G scattered under.
+template <int DIM, typename T>
+int op_substeps_fused(const ffmpm_params& p, const Layout& L, const Ws& w, PView<T> va, PView<T> vb, int32_t* ids_a,
+                      int32_t* ids_b, int nsteps, cudaStream_t s, PhaseTimer* tm) {
+  const int K = sort_every(p);
+  const uint32_t* flag = &w.hdr->sort_now;
+  const uint32_t* perm = nullptr;
+  k_sort_decide<<<1, 1, 0, s>>>(w.hdr, 1);
+  sort_and_plan<DIM, T>(p, L, w, va, false, &perm, s, tm, flag);
+  if (tm) tm->begin(3);
+  launch_p2g<DIM, T>(p, L, w, va, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s, flag);
+  if (tm) tm->end(1);
+  for (int k = 0; k < nsteps; ++k) {
+    const PView<T>& in = (k & 1) ? vb : va;
+    const PView<T>& out = (k & 1) ? va : vb;
+    const int32_t* ids_in = (k & 1) ? ids_b : ids_a;
+    int32_t* ids_out = (k & 1) ? ids_a : ids_b;
+    if (tm) tm->begin(4);
+    launch_grid_update<DIM, T>(p, L, w, s);
+    if (tm) tm->end(1);
+    if (k == nsteps - 1) {
+      // the buffer holds the order of the current plan: G2P must not apply the last permutation again
+      if (k > 0) cudaMemsetAsync(&w.hdr->sort_now, 0, sizeof(uint32_t), s);
+      G2PExtra ex{ids_in, ids_out, w.keys_next, w.block_count, L.cell_bits, w.gridB, nullptr, 0};
+      if (tm) tm->begin(5);
+      const int rc = launch_g2p<DIM, T, true, true>(p, L, w, in, out, perm, nullptr, ex, s, flag);
+      if (tm) tm->end(1);
+      if (rc != FFMPM_OK) return rc;
+      break;
+    }
+    if (k > 0) {
+      k_sort_decide<<<1, 1, 0, s>>>(w.hdr, k % K == 0 ? 1 : 0);
+      sort_and_plan<DIM, T>(p, L, w, in, true, &perm, s, tm, flag);
+    }
+    G2PExtra ex{ids_in, ids_out, w.keys_next, w.block_count, L.cell_bits, w.gridB, &w.hdr->far_stray, 1};
+    if (tm) tm->begin(6);
+    const int rc = launch_g2p2g<DIM, T>(p, L, w, in, out, perm, ex, s, flag);
+    if (tm) tm->end(1);
+    if (rc != FFMPM_OK) return rc;
+  }
+  cudaMemsetAsync(w.block_count, 0, sizeof(uint32_t) * L.nblocks, s);
+  return check_launch();
+}
+
 template <int DIM, typename T>
 int op_substeps_sorted(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_particles* a, ffmpm_particles* b,
                        int32_t* ids_a, int32_t* ids_b, int nsteps, cudaStream_t s, PhaseTimer* tm = nullptr) {
   PView<T> va = pview<T>(*a), vb = pview<T>(*b);
+  if (fused(p, nsteps)) return op_substeps_fused<DIM, T>(p, L, w, va, vb, ids_a, ids_b, nsteps, s, tm);
   const int K = sort_every(p);
   const uint32_t* flag = K > 1 ? &w.hdr->sort_now : nullptr;
   for (int k = 0; k < nsteps; ++k) {
@@ -408,7 +479,7 @@ int op_substeps_sorted(const ffmpm_params& p, const Layout& L, const Ws& w, ffmp
       launch_grid_update<DIM, T>(p, L, w, s);
     if (tm) tm->end(1);
     G2PExtra ex{ids_in, ids_out, w.keys_next, w.block_count, L.cell_bits, flag ? w.gridB : nullptr,
-                flag ? &w.hdr->far_stray : nullptr};
+                flag ? &w.hdr->far_stray : nullptr, 0};
     if (tm) tm->begin(5);
     int rc = launch_g2p<DIM, T, true, true>(p, L, w, in, out, perm, nullptr, ex, s, flag);
     if (tm) tm->end(1);
@@ -634,6 +705,23 @@ int ffmpm_plan_info(const ffmpm_params* p, int64_t n, int64_t* info) {
   info[5] = L.passes + 5 + (sort_every(*p) > 1 ? 1 : 0);
   info[6] = L.tile;
   info[7] = L.max_chunks;
+  return FFMPM_OK;
+}
+
+int ffmpm_kernels_per_call(const ffmpm_params* p, int64_t n, int32_t nsteps, int64_t* count) {
+  Layout L;
+  if (!p || !count || nsteps < 0 || !make_layout(*p, n, &L)) return FFMPM_ERR_BADARG;
+  const int64_t sort = 1 + L.passes + 1;  // digit histogram, one kernel per pass, plan
+  if (n == 0 || nsteps == 0) {
+    *count = 0;
+  } else if (fused(*p, nsteps)) {
+    // decide + keys + sort + P2G; per substep k < n-1: grid update (+ decide + sort for k > 0) +
+    // fused kernel; the last substep: grid update + G2P
+    *count = (1 + 1 + sort + 1) + 2 + int64_t(nsteps - 2) * (1 + 1 + sort + 1) + 2;
+  } else {
+    // per substep: (decide) + sort + P2G + grid update + G2P; keys once
+    *count = int64_t(nsteps) * ((sort_every(*p) > 1 ? 1 : 0) + sort + 3) + 1;
+  }
   return FFMPM_OK;
 }
 

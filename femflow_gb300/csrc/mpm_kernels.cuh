@@ -29,6 +29,7 @@ struct KParams {
 // Variant flags (ffmpm_params.variant).
 constexpr int kVariantP2GDirect = 1;  // P2G scatters straight to L2 with vector reds (no smem tile)
 constexpr int kVariantP2GLanes = 2;   // P2G lane-per-particle shared-tile atomics (no cell runs)
+constexpr int kVariantNoFuse = 4;     // sorted solver: separate G2P and P2G launches every substep
 constexpr int kVariantSortShift = 8;  // bits 8..15: substeps between re-sorts of the sorted solver
 
 template <typename T>
@@ -190,8 +191,8 @@ template <int DIM>
 __global__ void __launch_bounds__(1024) k_plan(Geom<DIM> g, uint32_t* __restrict__ block_count,
                                                uint32_t* __restrict__ block_start, uint32_t* __restrict__ block_cnt,
                                                int4* __restrict__ chunks, uint32_t* __restrict__ touched,
-                                               int4* __restrict__ occupied, WsHeader* hdr,
-                                               const uint32_t* __restrict__ sort_flag, int sym) {
+                                               uint32_t* __restrict__ tmark, int4* __restrict__ occupied,
+                                               WsHeader* hdr, const uint32_t* __restrict__ sort_flag, int sym) {
   if (sort_flag && *sort_flag == 0u) {
     // no re-sort this substep: keep the plan, only clear the histogram G2P accumulates
     for (int b = threadIdx.x; b < g.nblocks; b += blockDim.x) block_count[b] = 0;
@@ -260,6 +261,7 @@ __global__ void __launch_bounds__(1024) k_plan(Geom<DIM> g, uint32_t* __restrict
         chunks[carry.b + ex.b + q] = make_int4(b, (int)s, (int)min((uint32_t)kChunk, c - q * kChunk), 0);
       }
       if (tch) touched[carry.c + ex.c] = (uint32_t)b;
+      tmark[b] = tch;
       if (c > 0) occupied[carry.d + ex.d] = make_int4(b, (int)start, (int)c, 0);
     }
     carry.a += tot.a; carry.b += tot.b; carry.c += tot.c; carry.d += tot.d;
@@ -689,6 +691,260 @@ __device__ void p2g_scatter_record(const T* rec, int R, const Sink& sink) {
       }
 }
 
+// Shared-memory arrays of the cell-run P2G (phases 2 and 3).
+template <typename T>
+struct CellRunSmem {
+  T* recs;     // [kChunk][RecLayout::kStride]
+  int* cells;  // [kChunk] cell of each record (negative: no tile contribution)
+  int* rank;   // [kChunk]
+  int* order;  // [kChunk]
+  int* runs;   // [max(kChunk, ncell) + 1]
+  int* hist;   // [ncell]
+  int* nruns;  // 1
+  int* warp_cnt;
+  int* warp_nz;  // [kThreads / 32] each
+};
+
+// Bytes of the cell-run arrays (records + the int arrays) after the tile, for block side bs.
+template <int DIM, typename T>
+__host__ __device__ constexpr size_t cell_run_smem_bytes(int bs) {
+  const int ncell = DIM == 3 ? bs * bs * bs : bs * bs;
+  return size_t(kChunk) * RecLayout<DIM>::kStride * sizeof(T) +
+         sizeof(int) * (3 * kChunk + (kChunk > ncell ? kChunk : ncell) + 1 + ncell);
+}
+
+template <int DIM, typename T>
+__device__ __forceinline__ CellRunSmem<T> cell_run_smem(unsigned char* at, const Geom<DIM>& g, int* nruns,
+                                                        int* warp_cnt, int* warp_nz) {
+  const int ncell = DIM == 3 ? g.bs * g.bs * g.bs : g.bs * g.bs;
+  CellRunSmem<T> cr;
+  cr.recs = reinterpret_cast<T*>(at);
+  cr.cells = reinterpret_cast<int*>(cr.recs + (size_t)kChunk * RecLayout<DIM>::kStride);
+  cr.rank = cr.cells + kChunk;
+  cr.order = cr.rank + kChunk;
+  cr.runs = cr.order + kChunk;
+  cr.hist = cr.runs + max(kChunk, ncell) + 1;
+  cr.nruns = nruns;
+  cr.warp_cnt = warp_cnt;
+  cr.warp_nz = warp_nz;
+  return cr;
+}
+
+// Phase-1 tail: store record `rec` (of kind kRecTile / kRecStray / kRecOut) as record l.  Cell -1
+// marks a particle outside the grid, -2 one whose stencil left the block's tile (scattered to the
+// global grid after the phase; its base node rides in the record's padding).
+template <int DIM, typename T>
+__device__ __forceinline__ void p2g_store_record(const CellRunSmem<T>& cr, int l, T* rec, int kind, int cell,
+                                                 const int base[DIM]) {
+  constexpr int RF = RecLayout<DIM>::kFloats;
+  constexpr int RS = RecLayout<DIM>::kStride;
+#pragma unroll
+  for (int i = RF; i < RS; ++i) rec[i] = T(0);
+  if (kind == kRecStray) {
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) rec[RF + d] = T(base[d]);
+    cell = -2;
+  } else if (kind != kRecTile) {
+    cell = -1;
+  }
+  Node4<T>* dst = reinterpret_cast<Node4<T>*>(cr.recs + (size_t)l * RS);
+#pragma unroll
+  for (int i = 0; i < RS / 4; ++i) dst[i] = Node4<T>{rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]};
+  cr.cells[l] = cell;
+}
+
+// Phases 2 and 3 of the cell-run P2G over the nrec records of one chunk (phase 1 has filled
+// recs/cells and synchronised): group the records by cell, then add every cell's run to the tile.
+// Ends with the tile adds issued (no trailing barrier).
+template <int DIM, typename T>
+__device__ __forceinline__ void p2g_cell_runs(const CellRunSmem<T>& cr, const Geom<DIM>& g, int nrec,
+                                              const TileAdder<DIM, T>& tacc) {
+  constexpr int RS = RecLayout<DIM>::kStride;
+  const int ncell = DIM == 3 ? g.bs * g.bs * g.bs : g.bs * g.bs;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* const recs = cr.recs;
+  int* const cells = cr.cells;
+  int* const rank = cr.rank;
+  int* const order = cr.order;
+  int* const runs = cr.runs;
+  int* const hist = cr.hist;
+  int* const warp_cnt = cr.warp_cnt;
+  int* const warp_nz = cr.warp_nz;
+  // phase 2: group the chunk's particles by cell with a counting sort in shared memory (the
+  // chunk's order can come from a re-sort several substeps old, so equal cells need not be
+  // adjacent).  Run r is order[runs[r] .. runs[r + 1]): the particles of one cell.  Particles
+  // with cell -1 (outside the grid, or strays handled in phase 1) are left out.
+  {
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) hist[c] = 0;
+    __syncthreads();
+    // one shared atomic per distinct cell of a warp (neighbouring particles mostly share a cell)
+    for (int l = threadIdx.x; l < nrec; l += blockDim.x) {
+      const int c = cells[l];
+      const unsigned act = __activemask();
+      const unsigned peers = __match_any_sync(act, c);
+      const int leader = __ffs(peers) - 1;
+      int first = 0;
+      if (c >= 0 && lane == leader) first = atomicAdd(&hist[c], __popc(peers));
+      first = __shfl_sync(peers, first, leader);
+      rank[l] = c >= 0 ? first + __popc(peers & lanemask_lt()) : -1;
+    }
+    __syncthreads();
+    const int per_t = (ncell + blockDim.x - 1) / blockDim.x;
+    const int beg = threadIdx.x * per_t;
+    const int end = min(ncell, beg + per_t);
+    int cnt = 0, nz = 0;
+    for (int c = beg; c < end; ++c) {
+      cnt += hist[c];
+      nz += hist[c] > 0;
+    }
+    int icnt = cnt, inz = nz;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int tc = __shfl_up_sync(0xffffffffu, icnt, o), tz = __shfl_up_sync(0xffffffffu, inz, o);
+      if (lane >= o) {
+        icnt += tc;
+        inz += tz;
+      }
+    }
+    if (lane == 31) {
+      warp_cnt[warp] = icnt;
+      warp_nz[warp] = inz;
+    }
+    __syncthreads();
+    int pos = 0, r = 0, tot_cnt = 0, tot_nz = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+      pos += w < warp ? warp_cnt[w] : 0;
+      r += w < warp ? warp_nz[w] : 0;
+      tot_cnt += warp_cnt[w];
+      tot_nz += warp_nz[w];
+    }
+    pos += icnt - cnt;
+    r += inz - nz;
+    for (int c = beg; c < end; ++c) {
+      const int h = hist[c];
+      if (h > 0) runs[r++] = pos;
+      hist[c] = pos;  // start of cell c in order[]
+      pos += h;
+    }
+    if (threadIdx.x == 0) {
+      *cr.nruns = tot_nz;
+      runs[tot_nz] = tot_cnt;
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < nrec; l += blockDim.x) {
+      const int c = cells[l];
+      if (c >= 0) order[hist[c] + rank[l]] = l;
+    }
+  }
+  __syncthreads();
+  const int nruns = *cr.nruns;
+  // phase 3: a warp per run.  A particle is served by LP lanes (3D: 9, one per (j, k); 2D: 3, one
+  // per j); each lane accumulates the 3 nodes along x (i = 0, 1, 2) of its (j, k), and the warp
+  // takes NG particles of the run per step.  The NG partial sums are then folded onto group 0.
+  constexpr int LP = DIM == 3 ? 9 : 3;
+  constexpr int NG = 32 / LP;  // 3 (3D) or 10 (2D) particles per step
+  const int grp = lane / LP;
+  const int jk = lane - grp * LP;
+  const bool active = grp < NG;
+  const int oj = DIM == 3 ? jk / 3 : jk, ok = DIM == 3 ? jk % 3 : 0;
+  constexpr int a0 = 1 + DIM;
+  constexpr int w0 = RecLayout<DIM>::kW;
+  for (int r = warp; r < nruns; r += kThreads / 32) {
+    const int l0 = runs[r], l1 = runs[r + 1];
+    T acc[3][4];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = T(0);
+    if (active) {
+      // a lane needs m, q, dx A and the x weights (the first RU floats: whole float4s) and its own
+      // y (and z) weight; two records per step, both loaded before either is accumulated
+      constexpr int RU = DIM == 3 ? 16 : 12;
+      struct Rv {
+        T v[RU];
+        T wjk;
+      };
+      auto load = [&](int ll, Rv& rv) {
+        const T* rc = recs + (size_t)order[ll] * RS;
+        const Node4<T>* src = reinterpret_cast<const Node4<T>*>(rc);
+#pragma unroll
+        for (int i = 0; i < RU / 4; ++i) {
+          const Node4<T> q4 = src[i];
+          rv.v[4 * i] = q4.x;
+          rv.v[4 * i + 1] = q4.y;
+          rv.v[4 * i + 2] = q4.z;
+          rv.v[4 * i + 3] = q4.w;
+        }
+        if constexpr (DIM == 3)
+          rv.wjk = rc[w0 + 3 + oj] * rc[w0 + 6 + ok];
+        else
+          rv.wjk = rc[w0 + 3 + oj];
+      };
+      auto accum = [&](const Rv& r) {
+        const T* rv = r.v;
+        const T m = rv[0];
+        const T wjk = r.wjk;
+        // base_r = q_r + a_r1 j (+ a_r2 k); node i adds i * a_r0
+        T base[DIM], step[DIM];
+#pragma unroll
+        for (int rr = 0; rr < DIM; ++rr) {
+          T b = rv[1 + rr] + rv[a0 + rr * DIM + 1] * T(oj);
+          if constexpr (DIM == 3) b += rv[a0 + rr * DIM + 2] * T(ok);
+          base[rr] = b;
+          step[rr] = rv[a0 + rr * DIM];
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const T wgt = rv[w0 + i] * wjk;
+#pragma unroll
+          for (int rr = 0; rr < DIM; ++rr) acc[i][rr] += wgt * (base[rr] + T(i) * step[rr]);
+          acc[i][3] += wgt * m;
+        }
+      };
+      int ll = l0 + grp;
+      for (; ll + NG < l1; ll += 2 * NG) {
+        Rv ra, rb;
+        load(ll, ra);
+        load(ll + NG, rb);
+        accum(ra);
+        accum(rb);
+      }
+      if (ll < l1) {
+        Rv ra;
+        load(ll, ra);
+        accum(ra);
+      }
+    }
+    // fold the NG groups onto group 0 (lanes 0..LP-1)
+#pragma unroll
+    for (int off = 1; off < NG; off <<= 1) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const T t = __shfl_down_sync(0xffffffffu, acc[i][c], off * LP);
+          if (grp % (2 * off) == 0 && grp + off < NG) acc[i][c] += t;
+        }
+    }
+    if (grp == 0) {
+      const int cl = cells[order[l0]];
+      int lb[DIM];
+      if constexpr (DIM == 3) {
+        lb[2] = cl % g.bs;
+        lb[1] = (cl / g.bs) % g.bs;
+        lb[0] = cl / (g.bs * g.bs);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+          tacc.add(lb[0] + i, lb[1] + oj, lb[2] + ok, acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+      } else {
+        lb[1] = cl % g.bs;
+        lb[0] = cl / g.bs;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) tacc.add(lb[0] + i, lb[1] + oj, 0, acc[i][0], acc[i][1], T(0), acc[i][3]);
+      }
+    }
+  }
+}
+
 template <int DIM, typename T, typename Sink>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(KParams<T> kp, Geom<DIM> g, PView<T> P,
                                                         const uint32_t* __restrict__ perm,
@@ -696,22 +952,15 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
                                                         const WsHeader* __restrict__ hdr, Sink sink, int32_t* status,
                                                         uint32_t* fallbacks, const uint32_t* __restrict__ sort_flag) {
   if (sort_flag && *sort_flag == 0u) perm = nullptr;  // plan kept from an earlier substep: identity order
-  constexpr int RF = RecLayout<DIM>::kFloats;
   constexpr int RS = RecLayout<DIM>::kStride;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int TN = tile_nodes<DIM>(g);
   T* tile = reinterpret_cast<T*>(smem_raw);
-  T* recs = tile + 4 * TN;                                          // [kChunk][RS]
-  int* cells = reinterpret_cast<int*>(recs + (size_t)kChunk * RS);  // [kChunk]
-  const int ncell = DIM == 3 ? g.bs * g.bs * g.bs : g.bs * g.bs;
-  int* rank = cells + kChunk;                                       // [kChunk]
-  int* order = rank + kChunk;                                       // [kChunk]
-  int* runs = order + kChunk;                                       // [max(kChunk, ncell) + 1]
-  int* hist = runs + max(kChunk, ncell) + 1;                        // [ncell]
   __shared__ int nruns_s;
   __shared__ int warp_cnt[kThreads / 32];
   __shared__ int warp_nz[kThreads / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const CellRunSmem<T> cr = cell_run_smem<DIM, T>(reinterpret_cast<unsigned char*>(tile + 4 * TN), g, &nruns_s,
+                                                  warp_cnt, warp_nz);
   const uint32_t nch = hdr->n_chunks;
   const uint32_t per = (nch + gridDim.x - 1) / gridDim.x;
   const uint32_t c0 = blockIdx.x * per;
@@ -734,8 +983,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
 #pragma unroll
       for (int d = 0; d < DIM; ++d) org[d] = bc[d] * g.bs;
     }
-    // phase 1: one record per particle and thread (cell -1 marks a particle that failed the bounds
-    // check, -2 one whose stencil left the block's tile).  One particle at a time: two in flight per
+    // phase 1: one record per particle and thread.  One particle at a time: two in flight per
     // thread cost more registers than their overlapped loads gain.
     for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {
       const uint32_t s = ch.y + l;
@@ -744,198 +992,13 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
       T rec[RS];
       int cell = -1, base[DIM];
       const int kind = p2g_record<DIM, T>(kp, g, in, org, rec, cell, status, fallbacks, base);
-#pragma unroll
-      for (int i = RF; i < RS; ++i) rec[i] = T(0);
-      if (kind == kRecStray) {
-        // scattered after the phase (below); its base node rides in the record's padding
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) rec[RF + d] = T(base[d]);
-        cell = -2;
-      } else if (kind != kRecTile) {
-        cell = -1;
-      }
-      Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)l * RS);
-#pragma unroll
-      for (int i = 0; i < RS / 4; ++i) dst[i] = Node4<T>{rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]};
-      cells[l] = cell;
+      p2g_store_record<DIM, T>(cr, l, rec, kind, cell, base);
     }
     __syncthreads();
     // particles whose stencil left the block's tile (only between re-sorts): direct global adds
     for (int l = threadIdx.x; l < ch.z; l += blockDim.x)
-      if (cells[l] == -2) p2g_scatter_record<DIM, T, Sink>(recs + (size_t)l * RS, g.R, sink);
-    // phase 2: group the chunk's particles by cell with a counting sort in shared memory (the
-    // chunk's order can come from a re-sort several substeps old, so equal cells need not be
-    // adjacent).  Run r is order[runs[r] .. runs[r + 1]): the particles of one cell.  Particles
-    // with cell -1 (outside the grid, or strays handled in phase 1) are left out.
-    {
-      for (int c = threadIdx.x; c < ncell; c += blockDim.x) hist[c] = 0;
-      __syncthreads();
-      // one shared atomic per distinct cell of a warp (neighbouring particles mostly share a cell)
-      for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {
-        const int c = cells[l];
-        const unsigned act = __activemask();
-        const unsigned peers = __match_any_sync(act, c);
-        const int leader = __ffs(peers) - 1;
-        int first = 0;
-        if (c >= 0 && lane == leader) first = atomicAdd(&hist[c], __popc(peers));
-        first = __shfl_sync(peers, first, leader);
-        rank[l] = c >= 0 ? first + __popc(peers & lanemask_lt()) : -1;
-      }
-      __syncthreads();
-      const int per_t = (ncell + blockDim.x - 1) / blockDim.x;
-      const int beg = threadIdx.x * per_t;
-      const int end = min(ncell, beg + per_t);
-      int cnt = 0, nz = 0;
-      for (int c = beg; c < end; ++c) {
-        cnt += hist[c];
-        nz += hist[c] > 0;
-      }
-      int icnt = cnt, inz = nz;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int tc = __shfl_up_sync(0xffffffffu, icnt, o), tz = __shfl_up_sync(0xffffffffu, inz, o);
-        if (lane >= o) {
-          icnt += tc;
-          inz += tz;
-        }
-      }
-      if (lane == 31) {
-        warp_cnt[warp] = icnt;
-        warp_nz[warp] = inz;
-      }
-      __syncthreads();
-      int pos = 0, r = 0, tot_cnt = 0, tot_nz = 0;
-#pragma unroll
-      for (int w = 0; w < kThreads / 32; ++w) {
-        pos += w < warp ? warp_cnt[w] : 0;
-        r += w < warp ? warp_nz[w] : 0;
-        tot_cnt += warp_cnt[w];
-        tot_nz += warp_nz[w];
-      }
-      pos += icnt - cnt;
-      r += inz - nz;
-      for (int c = beg; c < end; ++c) {
-        const int h = hist[c];
-        if (h > 0) runs[r++] = pos;
-        hist[c] = pos;  // start of cell c in order[]
-        pos += h;
-      }
-      if (threadIdx.x == 0) {
-        nruns_s = tot_nz;
-        runs[tot_nz] = tot_cnt;
-      }
-      __syncthreads();
-      for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {
-        const int c = cells[l];
-        if (c >= 0) order[hist[c] + rank[l]] = l;
-      }
-    }
-    __syncthreads();
-    const int nruns = nruns_s;
-    // phase 3: a warp per run.  A particle is served by LP lanes (3D: 9, one per (j, k); 2D: 3, one
-    // per j); each lane accumulates the 3 nodes along x (i = 0, 1, 2) of its (j, k), and the warp
-    // takes NG particles of the run per step.  The NG partial sums are then folded onto group 0.
-    constexpr int LP = DIM == 3 ? 9 : 3;
-    constexpr int NG = 32 / LP;  // 3 (3D) or 10 (2D) particles per step
-    const int grp = lane / LP;
-    const int jk = lane - grp * LP;
-    const bool active = grp < NG;
-    const int oj = DIM == 3 ? jk / 3 : jk, ok = DIM == 3 ? jk % 3 : 0;
-    constexpr int a0 = 1 + DIM;
-    constexpr int w0 = RecLayout<DIM>::kW;
-    for (int r = warp; r < nruns; r += kThreads / 32) {
-      const int l0 = runs[r], l1 = runs[r + 1];
-      T acc[3][4];
-#pragma unroll
-      for (int i = 0; i < 3; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = T(0);
-      if (active) {
-        // a lane needs m, q, dx A and the x weights (the first RU floats: whole float4s) and its own
-        // y (and z) weight; two records per step, both loaded before either is accumulated
-        constexpr int RU = DIM == 3 ? 16 : 12;
-        struct Rv {
-          T v[RU];
-          T wjk;
-        };
-        auto load = [&](int ll, Rv& rv) {
-          const T* rc = recs + (size_t)order[ll] * RS;
-          const Node4<T>* src = reinterpret_cast<const Node4<T>*>(rc);
-#pragma unroll
-          for (int i = 0; i < RU / 4; ++i) {
-            const Node4<T> q4 = src[i];
-            rv.v[4 * i] = q4.x;
-            rv.v[4 * i + 1] = q4.y;
-            rv.v[4 * i + 2] = q4.z;
-            rv.v[4 * i + 3] = q4.w;
-          }
-          if constexpr (DIM == 3)
-            rv.wjk = rc[w0 + 3 + oj] * rc[w0 + 6 + ok];
-          else
-            rv.wjk = rc[w0 + 3 + oj];
-        };
-        auto accum = [&](const Rv& r) {
-          const T* rv = r.v;
-          const T m = rv[0];
-          const T wjk = r.wjk;
-          // base_r = q_r + a_r1 j (+ a_r2 k); node i adds i * a_r0
-          T base[DIM], step[DIM];
-#pragma unroll
-          for (int rr = 0; rr < DIM; ++rr) {
-            T b = rv[1 + rr] + rv[a0 + rr * DIM + 1] * T(oj);
-            if constexpr (DIM == 3) b += rv[a0 + rr * DIM + 2] * T(ok);
-            base[rr] = b;
-            step[rr] = rv[a0 + rr * DIM];
-          }
-#pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            const T wgt = rv[w0 + i] * wjk;
-#pragma unroll
-            for (int rr = 0; rr < DIM; ++rr) acc[i][rr] += wgt * (base[rr] + T(i) * step[rr]);
-            acc[i][3] += wgt * m;
-          }
-        };
-        int ll = l0 + grp;
-        for (; ll + NG < l1; ll += 2 * NG) {
-          Rv ra, rb;
-          load(ll, ra);
-          load(ll + NG, rb);
-          accum(ra);
-          accum(rb);
-        }
-        if (ll < l1) {
-          Rv ra;
-          load(ll, ra);
-          accum(ra);
-        }
-      }
-      // fold the NG groups onto group 0 (lanes 0..LP-1)
-#pragma unroll
-      for (int off = 1; off < NG; off <<= 1) {
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const T t = __shfl_down_sync(0xffffffffu, acc[i][c], off * LP);
-            if (grp % (2 * off) == 0 && grp + off < NG) acc[i][c] += t;
-          }
-      }
-      if (grp == 0) {
-        const int cl = cells[order[l0]];
-        int lb[DIM];
-        if constexpr (DIM == 3) {
-          lb[2] = cl % g.bs;
-          lb[1] = (cl / g.bs) % g.bs;
-          lb[0] = cl / (g.bs * g.bs);
-#pragma unroll
-          for (int i = 0; i < 3; ++i)
-            tacc.add(lb[0] + i, lb[1] + oj, lb[2] + ok, acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
-        } else {
-          lb[1] = cl % g.bs;
-          lb[0] = cl / g.bs;
-#pragma unroll
-          for (int i = 0; i < 3; ++i) tacc.add(lb[0] + i, lb[1] + oj, 0, acc[i][0], acc[i][1], T(0), acc[i][3]);
-        }
-      }
-    }
+      if (cr.cells[l] == -2) p2g_scatter_record<DIM, T, Sink>(cr.recs + (size_t)l * RS, g.R, sink);
+    p2g_cell_runs<DIM, T>(cr, g, ch.z, tacc);
     __syncthreads();  // records and runs are rewritten by the next chunk
   }
   if (cur >= 0) {
@@ -1394,6 +1457,10 @@ struct G2PExtra {
   // +-1 of that block (the next substep must then re-sort)
   const void* grid_global;
   uint32_t* far_flag;
+  // cells by which the far test is tightened: 1 when the next scatter of the same particle happens
+  // before the next re-sort can take effect (fused G2P + P2G), so that a particle moving less than a
+  // cell per substep never needs the touched-block fix-up
+  int far_margin;
 };
 
 // The state G2P reads of one particle (loaded ahead of the arithmetic so that the loads of
@@ -1414,11 +1481,16 @@ __device__ __forceinline__ void g2p_load(const PView<T>& Pin, uint32_t p, bool n
   in.jp = need_jp ? Pin.Jp[p] : T(1);
 }
 
-template <int DIM, typename T>
-__device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DIM>& g, const PView<T>& Pin,
+// G2P of one particle p, written to slot q of Pout.  With kNext (fused G2P + P2G) the updated
+// particle also goes to *next (the input of the next substep's P2G), and v and C are not stored:
+// the next substep's G2P rebuilds them from the grid.  Returns false for a particle outside the grid
+// or off its tile without a global grid (nothing written).
+template <int DIM, typename T, bool kNext = false>
+__device__ __forceinline__ bool g2p_particle(const KParams<T>& kp, const Geom<DIM>& g, const PView<T>& Pin,
                                              const PView<T>& Pout, uint32_t p, uint32_t q, const int org[DIM],
                                              const Node4<T>* tile, int32_t* status, bool sorted,
-                                             const G2PExtra& ex, const G2PIn<DIM, T>& in) {
+                                             const G2PExtra& ex, const G2PIn<DIM, T>& in,
+                                             P2GIn<DIM, T>* next = nullptr) {
   constexpr int DD = DIM * DIM;
   T xp[DIM], fx[DIM], w[3][DIM];
   int lb[DIM], base[DIM];
@@ -1437,7 +1509,7 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
   }
   if (!ok || (!in_tile && !ex.grid_global)) {
     raise_status(status, FFMPM_STATUS_OOB);
-    return;
+    return false;
   }
   // stencil source: the staged tile, or (a particle that left its chunk block's tile between
   // re-sorts) the global node grid.  Node (i, j[, k]) of the stencil is src[i s0 + j s1 (+ k s2)]:
@@ -1588,18 +1660,40 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     Pout.x[Pout.at(q, d, DIM)] = xn[d];
-    Pout.v[Pout.at(q, d, DIM)] = v[d];
+    if constexpr (!kNext) Pout.v[Pout.at(q, d, DIM)] = v[d];
   }
 #pragma unroll
   for (int i = 0; i < DD; ++i) {
-    Pout.C[Pout.at(q, i, DD)] = Cn[i];
+    if constexpr (!kNext) Pout.C[Pout.at(q, i, DD)] = Cn[i];
     Pout.F[Pout.at(q, i, DD)] = Fn[i];
   }
   if (write_jp) Pout.Jp[q] = jp_new;
+  if constexpr (kNext) {
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      next->x[d] = xn[d];
+      next->v[d] = v[d];
+    }
+#pragma unroll
+    for (int i = 0; i < DD; ++i) {
+      next->F[i] = Fn[i];
+      next->C[i] = Cn[i];
+    }
+    next->m = Pin.mass ? Pin.mass[p] : kp.mass;
+    next->mu0 = Pin.mu0 ? Pin.mu0[p] : kp.mu0;
+    next->lam0 = Pin.lam0 ? Pin.lam0[p] : kp.lam0;
+    next->jp = kp.model == FFMPM_MODEL_SNOW ? jp_new : T(1);
+  }
   if (sorted) {
-    if (Pin.mass) Pout.mass[q] = Pin.mass[p];
-    if (Pin.mu0) Pout.mu0[q] = Pin.mu0[p];
-    if (Pin.lam0) Pout.lam0[q] = Pin.lam0[p];
+    if constexpr (kNext) {
+      if (Pin.mass) Pout.mass[q] = next->m;
+      if (Pin.mu0) Pout.mu0[q] = next->mu0;
+      if (Pin.lam0) Pout.lam0[q] = next->lam0;
+    } else {
+      if (Pin.mass) Pout.mass[q] = Pin.mass[p];
+      if (Pin.mu0) Pout.mu0[q] = Pin.mu0[p];
+      if (Pin.lam0) Pout.lam0[q] = Pin.lam0[p];
+    }
     if (ex.ids_in) ex.ids_out[q] = ex.ids_in[p];
     if (ex.keys_next) {
       // key of the updated position: the next substep's sort input (fused to avoid re-reading x)
@@ -1616,12 +1710,13 @@ __device__ __forceinline__ void g2p_particle(const KParams<T>& kp, const Geom<DI
           T fn;
           base_of(xn[d], kp.inv_dx, kp.res, bn, fn);
           const int l = bn - org[d];
-          far = far || l < -g.bs || l > 2 * g.bs - 3;
+          far = far || l < -g.bs + ex.far_margin || l > 2 * g.bs - 3 - ex.far_margin;
         }
         if (far) *ex.far_flag = 1u;
       }
     }
   }
+  return true;
 }
 
 template <int DIM, typename T, bool kTma, bool kSorted>
@@ -1720,6 +1815,151 @@ __global__ void __launch_bounds__(kThreads) k_g2p(KParams<T> kp, Geom<DIM> g, PV
       g2p_particle<DIM, T>(kp, g, Pin, Pout, p1, kSorted ? s1 : p1, org, tile, status, kSorted, ex, in1);
       if (two) g2p_particle<DIM, T>(kp, g, Pin, Pout, p2, kSorted ? s2 : p2, org, tile, status, kSorted, ex, in2);
     }
+  }
+}
+
+// ----------------------------------------------------------------------------------------------
+// Fused G2P + P2G: substep k's G2P and substep k+1's P2G in one pass over the particles.  The
+// updated particle (x, v, C, F) goes straight from the gather into the next substep's record, so
+// v and C never travel through memory between the two, and x and F are read once per substep.
+// Both halves use the chunk's block: the G2P tile of grid velocities (staged by TMA from the
+// workspace's velocity grid) and the P2G tile of momentum/mass (flushed into the workspace's
+// accumulation grid), and the cell-run phases of k_p2g_cells.  The block plan was made from the
+// positions of substep k, so a particle's new stencil may leave its block's tile (it takes the
+// direct global adds) or, moving fast, the blocks the plan touches: it then adds the blocks its
+// stencil covers to the touched list itself, so that the grid update visits every node that
+// received mass.
+
+// Add the blocks covered by the stencil at `base` to the touched list (each block once: `tmark`
+// holds 1 for every listed block).
+template <int DIM>
+__device__ __forceinline__ void mark_touched(const Geom<DIM>& g, const int base[DIM], uint32_t* tmark,
+                                             uint32_t* touched, uint32_t* n_touched) {
+  int lo[DIM], ext[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    lo[d] = base[d] / g.bs;
+    ext[d] = min((base[d] + 2) / g.bs, g.nb - 1) - lo[d];  // 0 or 1
+  }
+  for (int o = 0; o < (1 << DIM); ++o) {
+    int id = 0;
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      const int od = (o >> (DIM - 1 - d)) & 1;
+      ok = ok && od <= ext[d];
+      id = id * g.nb + lo[d] + od;
+    }
+    if (ok && atomicCAS(&tmark[id], 0u, 1u) == 0u) touched[atomicAdd(n_touched, 1u)] = (uint32_t)id;
+  }
+}
+
+// Dynamic shared memory of k_g2p2g: [pad to 128 B][G2P tile: TN Node4][mbarrier: 128 B]
+// [P2G tile: 4 TN reals][cell-run arrays], every region starting on 128 bytes.
+__host__ __device__ constexpr size_t align128(size_t v) { return (v + 127) & ~size_t(127); }
+
+template <int DIM, typename T>
+__host__ __device__ constexpr size_t g2p2g_smem_bytes(int TN, int bs) {
+  return 128 + align128(size_t(TN) * sizeof(Node4<T>)) + 128 + align128(size_t(4) * TN * sizeof(T)) +
+         cell_run_smem_bytes<DIM, T>(bs);
+}
+
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_g2p2g(
+    KParams<T> kp, Geom<DIM> g, PView<T> Pin, PView<T> Pout, const uint32_t* __restrict__ perm,
+    const int4* __restrict__ chunks, WsHeader* hdr, const __grid_constant__ CUtensorMap tmap, G2PExtra ex,
+    InternalSink<T> sink, uint32_t* __restrict__ tmark, uint32_t* __restrict__ touched, int32_t* status,
+    uint32_t* fallbacks, const uint32_t* __restrict__ sort_flag) {
+  if (sort_flag && *sort_flag == 0u) perm = nullptr;  // plan kept from an earlier substep: identity order
+  constexpr int RS = RecLayout<DIM>::kStride;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int TN = tile_nodes<DIM>(g);
+  unsigned char* at = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  Node4<T>* gtile = reinterpret_cast<Node4<T>*>(at);
+  at += align128(size_t(TN) * sizeof(Node4<T>));
+  uint64_t& bar = *reinterpret_cast<uint64_t*>(at);
+  at += 128;
+  T* ptile = reinterpret_cast<T*>(at);
+  at += align128(size_t(4) * TN * sizeof(T));
+  __shared__ int nruns_s;
+  __shared__ int warp_cnt[kThreads / 32];
+  __shared__ int warp_nz[kThreads / 32];
+  const CellRunSmem<T> cr = cell_run_smem<DIM, T>(at, g, &nruns_s, warp_cnt, warp_nz);
+  const TileAdder<DIM, T> tacc{ptile, TN, g.tile};
+  const uint32_t nch = hdr->n_chunks;
+  const uint32_t per = (nch + gridDim.x - 1) / gridDim.x;
+  const uint32_t c0 = blockIdx.x * per;
+  const uint32_t c1 = min(nch, c0 + per);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  uint32_t phase = 0;
+  int cur = -1;
+  int org[DIM];
+  for (uint32_t c = c0; c < c1; ++c) {
+    const int4 ch = chunks[c];
+    if (ch.x != cur) {
+      if (cur >= 0) {
+        __syncthreads();  // phase 3 of the previous chunk is done with the P2G tile
+        p2g_flush<DIM, T, InternalSink<T>>(ptile, TN, g, org, sink);
+      }
+      __syncthreads();  // every thread is done with both tiles
+      cur = ch.x;
+      int bc[DIM];
+      block_coords<DIM>(g, cur, bc);
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) org[d] = bc[d] * g.bs;
+      if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&bar, (uint32_t)(TN * sizeof(Node4<T>)));
+        if constexpr (DIM == 3)
+          tma_load_4d(gtile, &tmap, &bar, 0, org[2], org[1], org[0]);
+        else
+          tma_load_3d(gtile, &tmap, &bar, 0, org[1], org[0]);
+      }
+      for (int t = threadIdx.x; t < 4 * TN; t += blockDim.x) ptile[t] = T(0);
+      const bool timed_out = !mbar_wait(&bar, phase);
+      phase ^= 1u;
+      if (__syncthreads_or(timed_out)) {
+        raise_status(status, FFMPM_STATUS_TIMEOUT);
+        return;
+      }
+    }
+    // phase 1: G2P of substep k, then the record of substep k+1, one particle per thread
+    for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {
+      const uint32_t s = ch.y + l;
+      const uint32_t p = perm ? perm[s] : s;
+      G2PIn<DIM, T> in;
+      g2p_load<DIM, T>(Pin, p, true, in);
+      P2GIn<DIM, T> nx;
+      T rec[RS];
+      int cell = -1, base[DIM];
+      int kind = kRecOut;
+      if (g2p_particle<DIM, T, true>(kp, g, Pin, Pout, p, s, org, gtile, status, true, ex, in, &nx)) {
+        kind = p2g_record<DIM, T>(kp, g, nx, org, rec, cell, status, fallbacks, base);
+        if (kind == kRecStray) {
+          // outside the blocks within +-1 of the chunk's block (which the plan always touches)
+          bool far = false;
+#pragma unroll
+          for (int d = 0; d < DIM; ++d) {
+            const int lb = base[d] - org[d];
+            far = far || lb < -g.bs || lb > 2 * g.bs - 3;
+          }
+          if (far) mark_touched<DIM>(g, base, tmark, touched, &hdr->n_touched);
+        }
+      }
+      p2g_store_record<DIM, T>(cr, l, rec, kind, cell, base);
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < ch.z; l += blockDim.x)
+      if (cr.cells[l] == -2) p2g_scatter_record<DIM, T, InternalSink<T>>(cr.recs + (size_t)l * RS, g.R, sink);
+    p2g_cell_runs<DIM, T>(cr, g, ch.z, tacc);
+    __syncthreads();  // records and runs are rewritten by the next chunk
+  }
+  if (cur >= 0) {
+    __syncthreads();
+    p2g_flush<DIM, T, InternalSink<T>>(ptile, TN, g, org, sink);
   }
 }
 

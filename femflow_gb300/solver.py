@@ -136,7 +136,8 @@ class MPMSolver:
     def profile(self, nsteps: int) -> dict:
         """Run ``nsteps`` substeps with CUDA events around every phase (synchronises).
 
-        Returns {phase: (total_ms, launches)} for keys, sort, plan, p2g, grid_update, g2p.
+        Returns {phase: (total_ms, launches)} for keys, sort, plan, p2g, grid_update, g2p and g2p2g
+        (the fused G2P + next substep's P2G).
         """
         ms = (ctypes.c_double * N.NPHASES)()
         cnt = (ctypes.c_int64 * N.NPHASES)()
@@ -156,6 +157,12 @@ class MPMSolver:
         keys = ("block_size", "blocks_per_axis", "blocks", "key_bits", "radix_passes", "kernels_per_substep",
                 "tile", "max_chunks")
         return dict(zip(keys, list(info)))
+
+    def kernels_per_call(self, nsteps: int) -> int:
+        """Kernels one call of ``nsteps`` substeps launches (as counted by the library)."""
+        c = ctypes.c_int64()
+        N.call("ffmpm_kernels_per_call", ctypes.byref(self.params), self.n, int(nsteps), ctypes.byref(c))
+        return int(c.value)
 
     # ------------------------------------------------------------------ state access
     def sorted_state(self):

@@ -138,16 +138,23 @@ int ffmpm_diagnostics_fp64(const ffmpm_params *p, const ffmpm_particles *P, doub
 /* Same as ffmpm_substeps_sorted, with CUDA events recorded around each phase on `stream`; the
  * call synchronises the stream and ADDS the per-phase milliseconds and launch counts into
  * phase_ms[FFMPM_NPHASES] / phase_launches[FFMPM_NPHASES] (host arrays).  Phases: 0 keys,
- * 1 sort, 2 plan, 3 P2G, 4 grid update, 5 G2P.  No reference counterpart (measurement only). */
-#define FFMPM_NPHASES 6
+ * 1 sort, 2 plan, 3 P2G, 4 grid update, 5 G2P, 6 fused G2P + next substep's P2G.  No reference
+ * counterpart (measurement only). */
+#define FFMPM_NPHASES 7
 int ffmpm_profile_substeps(const ffmpm_params *p, ffmpm_particles *a, ffmpm_particles *b, int32_t *ids_a,
                            int32_t *ids_b, int32_t nsteps, void *ws, size_t ws_bytes, void *stream,
                            double *phase_ms, int64_t *phase_launches);
 
 /* Host-only description of the work decomposition for (params, n): info[0] block side, [1] blocks
- * per axis, [2] blocks, [3] key bits, [4] radix passes, [5] kernels per sorted substep, [6] tile
- * side, [7] max work chunks.  No reference counterpart. */
+ * per axis, [2] blocks, [3] key bits, [4] radix passes, [5] kernels per substep of a sorted run
+ * with separate G2P and P2G launches, [6] tile side, [7] max work chunks.  No reference
+ * counterpart. */
 int ffmpm_plan_info(const ffmpm_params *p, int64_t n, int64_t *info);
+
+/* Number of kernels one ffmpm_substeps_sorted call of `nsteps` substeps on n particles launches
+ * (the kernels that return early on a substep without a re-sort included).  No reference
+ * counterpart (measurement only). */
+int ffmpm_kernels_per_call(const ffmpm_params *p, int64_t n, int32_t nsteps, int64_t *count);
 
 /* Largest n accepted by ffmpm_sort_by_block_static, and its error when n is larger. */
 #define FFMPM_STATIC_SORT_MAX_N 262144

@@ -66,7 +66,8 @@ def _scene(dtype, n_per=3000, res=32):
     return s
 
 
-@pytest.mark.parametrize("variant,sort_every", [(0, 1), (1, 1), (2, 1), (0, 3), (0, 8)])
+# variant 0 runs the fused G2P + P2G kernel, 4 separate G2P and P2G launches, 1 and 2 the P2G variants
+@pytest.mark.parametrize("variant,sort_every", [(0, 1), (1, 1), (2, 1), (0, 3), (0, 8), (4, 1), (4, 8)])
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_sorted_solver_matches_in_place_substeps(dtype, variant, sort_every):
     s = _scene(dtype)
@@ -118,6 +119,84 @@ def test_fast_particles_between_sorts(dtype):
     close(n(got["F"]), n(F), 10 * rel, scale=1.0, what="F")
     moved = np.abs(n(got["x"]) - x).max()
     assert moved * res > 12  # more than a block of 8 cells, ~10 cells between scheduled re-sorts
+
+
+def _fast_cluster(dim, n_, res, dt, cells_per_substep):
+    rng = np.random.default_rng(11)
+    centre = [0.2, 0.5, 0.45][:dim]
+    x = rng.uniform(-0.03, 0.03, (n_, dim)) + centre
+    v = np.zeros((n_, dim))
+    v[:, 0] = cells_per_substep / res / dt
+    v[:, -1] += 0.4 / res / dt
+    vol = 0.06 ** dim / n_
+    E_, nu = 1e3, 0.3
+    return x, v, vol, E_ / (2 * (1 + nu)), E_ * nu / ((1 + nu) * (1 - 2 * nu))
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_cluster_at_the_velocity_clamp(dtype):
+    """A 3D cluster launched at 2.5 cells per substep: the grid clamps every node velocity to
+    0.9 dx / dt (three_d/grid_op.py:25), so it crosses ~11 cells in 12 substeps with no scheduled
+    re-sort.  Only the far flags (raised a cell early in the fused G2P + P2G) re-sort it.  The
+    result equals the in-place substeps."""
+    n_, res, dt, g, steps = 3000, 64, 2e-4, -9.8, 12
+    x, v, vol, mu, lam = _fast_cluster(3, n_, res, dt, 2.5)
+    solver = MPMSolver(torch.tensor(x), res=res, dt=dt, gravity=g, volume=vol, mass=vol, mu_0=mu, lambda_0=lam,
+                       v=torch.tensor(v), dtype=dtype, sort_every=64)
+    solver.step(steps, check=True)
+    got = solver.state()
+    ps = ParticleSet(t(x, dtype), t(np.full(n_, vol), dtype), t(np.full(n_, mu), dtype), t(np.full(n_, lam), dtype))
+    vv, F, C, Jp = mls_mpm.make_mls_mpm_coefficients(n_, 3, dtype=dtype)
+    vv.copy_(t(v, dtype))
+    for _ in range(steps):
+        mls_mpm.solve_mls_mpm_3d(res, float(res), 1.0, 1 / res, dt, vol, g, ps, vv, F, C, Jp)
+    rel = 1e-12 if dtype == torch.float64 else 1e-5
+    close(n(got["x"]), n(ps.pos), rel, scale=1.0, what="x")
+    close(n(got["v"]), n(vv), 50 * rel, scale=float(np.abs(v).max()), what="v")
+    close(n(got["F"]), n(F), 10 * rel, scale=1.0, what="F")
+    assert (n(got["x"])[:, 0] - x[:, 0]).min() * res > 10.0
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_2d_cluster_faster_than_two_cells_per_substep(dtype):
+    """A 2D cluster at 2.5 cells per substep (the 2D grid rule has no velocity clamp,
+    two_d/grid_op.py): in the fused G2P + P2G a particle's new stencil leaves the blocks its plan
+    touches before the re-sort its far flag asks for takes effect, so the kernel adds those blocks
+    to the touched list itself.  Positions and velocities equal the in-place substeps."""
+    from femflow_gb300.solvers.mpm import two_d
+
+    n_, res, dt, g, steps = 3000, 64, 2e-4, -9.8, 12
+    x, v, vol, mu, lam = _fast_cluster(2, n_, res, dt, 2.5)
+    solver = MPMSolver(torch.tensor(x), res=res, dt=dt, gravity=g, volume=vol, mass=vol, mu_0=mu, lambda_0=lam,
+                       v=torch.tensor(v), dtype=dtype, sort_every=64)
+    solver.step(steps, check=True)
+    got = solver.state()
+    gx, gv = t(x, dtype), t(v, dtype)
+    gF, gC, gJ = t(np.tile(np.eye(2), (n_, 1, 1)), dtype), t(np.zeros((n_, 2, 2)), dtype), t(np.ones((n_, 1)), dtype)
+    for _ in range(steps):
+        two_d.solve_mls_mpm_2d(res, float(res), 1.0, mu, lam, vol, 1 / res, dt, vol, g, gx, gv, gF, gC, gJ)
+    rel = 1e-12 if dtype == torch.float64 else 1e-5
+    close(n(got["x"]), n(gx), rel, scale=1.0, what="x")
+    close(n(got["v"]), n(gv), 50 * rel, scale=float(np.abs(v).max()), what="v")
+    assert (n(got["x"])[:, 0] - x[:, 0]).min() * res > 2.4 * steps
+
+
+@pytest.mark.parametrize("variant", [0, 4])
+def test_fused_and_separate_launches(variant):
+    """Which kernels a sorted run launches: by default P2G once, then the fused G2P + P2G, and a
+    plain G2P for the last substep; with variant 4 a P2G and a G2P every substep."""
+    s = _scene(torch.float32)
+    solver = MPMSolver(torch.tensor(s["x"]), res=s["res"], dt=2e-4, gravity=-9.8, volume=s["vol"],
+                       mass=torch.tensor(s["mass"]), mu_0=torch.tensor(s["mu"]), lambda_0=torch.tensor(s["lam"]),
+                       v=torch.tensor(s["v"]), dtype=torch.float32, variant=variant)
+    prof = solver.profile(6)
+    launches = {k: v[1] for k, v in prof.items()}
+    if variant == 0:
+        assert (launches["p2g"], launches["g2p2g"], launches["g2p"]) == (1, 5, 1)
+    else:
+        assert (launches["p2g"], launches["g2p2g"], launches["g2p"]) == (6, 0, 6)
+    assert launches["grid_update"] == 6
+    solver.check()
 
 
 def test_graph_replay_matches_direct_launches():

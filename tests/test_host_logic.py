@@ -1,4 +1,6 @@
 """Host-side pieces that need no GPU: parameter packing, particle containers, helpers."""
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -51,3 +53,26 @@ def test_no_cpu_fallback_without_gpu():
     ps = PT.ParticleSet(torch.rand(4, 3) * 0.5 + 0.25, torch.ones(4), torch.ones(4), torch.ones(4))
     with pytest.raises(RuntimeError, match="CUDA"):
         mls_mpm.solve_mls_mpm_3d(16, 16.0, 1.0, 1 / 16, 1e-4, 1.0, -9.8, ps, v, F, C, Jp)
+
+
+def test_kernels_per_call():
+    """Launch counts of a sorted run (host-only query): fused G2P + P2G by default, separate G2P and
+    P2G launches for one substep and variant 4."""
+
+    def count(nsteps, **kw):
+        p = E.make_params(3, 128, torch.float32, 1 / 128, 128.0, 1e-4, **kw)
+        c = ctypes.c_int64()
+        N.call("ffmpm_kernels_per_call", ctypes.byref(p), 1 << 20, int(nsteps), ctypes.byref(c))
+        return c.value
+
+    info = (ctypes.c_int64 * 8)()
+    N.call("ffmpm_plan_info", ctypes.byref(E.make_params(3, 128, torch.float32, 1 / 128, 128.0, 1e-4)), 1 << 20, info)
+    sort = 1 + info[4] + 1  # digit histogram, radix passes, plan
+    every8 = 8 << 8
+    # fused: (decide, keys, sort, P2G) + 2 + (n - 2) (grid, decide, sort, fused) + (grid, G2P)
+    assert count(10, variant=every8) == (3 + sort) + 2 + 8 * (3 + sort) + 2
+    assert count(2, variant=every8) == (3 + sort) + 4
+    # one substep and variant 4: decide, sort, P2G, grid, G2P per substep, keys once
+    assert count(1, variant=every8) == 1 + sort + 3 + 1
+    assert count(10, variant=every8 | 4) == 10 * (1 + sort + 3) + 1
+    assert count(0, variant=every8) == 0
