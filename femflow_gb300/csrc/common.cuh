@@ -201,7 +201,16 @@ static __device__ __noinline__ void polar3_redo_fp64(const float* F, float* R, u
 template <typename T>
 __device__ __forceinline__ void polar3(const T F[9], T R[9], uint32_t* fallbacks) {
   if constexpr (sizeof(T) == 4) {
-    if (polar3_newton(F, R, 12, T(1e-3)) < 0) polar3_redo_fp64(F, R, fallbacks);
+    if (polar3_newton(F, R, 12, T(1e-3)) < 0) {
+      // copies made here, on the rare path, so that the call does not take the address of the
+      // caller's F and R (which would keep them in local memory for every particle)
+      float Fl[9], Rl[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) Fl[i] = F[i];
+      polar3_redo_fp64(Fl, Rl, fallbacks);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) R[i] = Rl[i];
+    }
   } else {
     // double: a failure means F is singular to working precision; the last iterate is kept (the
     // reference's LAPACK answer is arbitrary in the null space there) and counted.

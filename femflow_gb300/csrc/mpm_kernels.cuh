@@ -617,7 +617,7 @@ __device__ __forceinline__ int p2g_record(const KParams<T>& kp, const Geom<DIM>&
                                           const int org[DIM], T* rec, int& cell, int32_t* status,
                                           uint32_t* fallbacks, int base[DIM]) {
   constexpr int DD = DIM * DIM;
-  T fx[DIM], w[3][DIM];
+  T fx[DIM];
   int lb[DIM];
   bool ok = true, in_tile = true;
 #pragma unroll
@@ -627,11 +627,6 @@ __device__ __forceinline__ int p2g_record(const KParams<T>& kp, const Geom<DIM>&
     base[d] = b;
     lb[d] = b - org[d];
     in_tile = in_tile && lb[d] >= 0 && lb[d] + 2 < g.tile;
-    T ww[3];
-    bspline(fx[d], ww);
-    w[0][d] = ww[0];
-    w[1][d] = ww[1];
-    w[2][d] = ww[2];
   }
   if (!ok) {
     raise_status(status, FFMPM_STATUS_OOB);
@@ -654,11 +649,10 @@ __device__ __forceinline__ int p2g_record(const KParams<T>& kp, const Geom<DIM>&
   constexpr int a0 = DIM == 3 ? 4 : 3;
 #pragma unroll
   for (int i = 0; i < DD; ++i) rec[a0 + i] = dx * A[i];
+  // the weights last: they are not live during the stress
   constexpr int w0 = RecLayout<DIM>::kW;
 #pragma unroll
-  for (int d = 0; d < DIM; ++d)
-#pragma unroll
-    for (int i = 0; i < 3; ++i) rec[w0 + 3 * d + i] = w[i][d];
+  for (int d = 0; d < DIM; ++d) bspline(fx[d], rec + w0 + 3 * d);
   return in_tile ? kRecTile : kRecStray;
 }
 
