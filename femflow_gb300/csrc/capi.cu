@@ -256,11 +256,12 @@ __global__ void k_sort_decide(WsHeader* h, int periodic) {
 }
 
 // keys -> sort -> plan.  Leaves the permutation pointer in *perm.  With `flag` (cadenced runs) the
-// sort and the plan do their work only when the device word reads 1, and the plan dilates the
-// occupied blocks by +-1 so that it stays valid until the next re-sort.
+// sort and the plan do their work only when the device word reads 1.  With `sym` (default: with a
+// flag) the plan dilates the occupied blocks by +-1 so that it stays valid until the next re-sort.
 template <int DIM, typename T>
 void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const PView<T>& x, bool keys_ready,
-                   const uint32_t** perm, cudaStream_t s, PhaseTimer* tm = nullptr, const uint32_t* flag = nullptr) {
+                   const uint32_t** perm, cudaStream_t s, PhaseTimer* tm = nullptr, const uint32_t* flag = nullptr,
+                   int sym = -1) {
   const KParams<T> kp = kparams<T>(p);
   const Geom<DIM> g = geom<DIM>(L);
   const uint32_t n = (uint32_t)L.n;
@@ -277,7 +278,7 @@ void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const PV
   if (tm) tm->end(1 + L.passes);
   if (tm) tm->begin(2);
   k_plan<DIM><<<1, 1024, 0, s>>>(g, w.block_count, w.block_start, w.block_cnt, w.chunks, w.touched, w.tmark,
-                                 w.occupied, w.hdr, flag, flag ? 1 : 0);
+                                 w.occupied, w.hdr, flag, sym >= 0 ? sym : (flag ? 1 : 0));
   if (tm) tm->end(1);
 }
 
@@ -404,20 +405,24 @@ int op_substep(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_partic
 }
 
 // Substeps 0..n-1 with the fused kernel: P2G(0), then for k = 0..n-2: grid update(k), re-sort if
-// due, G2P(k) + P2G(k+1); then grid update(n-1) and G2P(n-1).  The state after every substep is
-// in buffer a or b as in the unfused loop (x, F, Jp, ids, per-particle material), with v and C
-// written by the last G2P only.  The grid update of substep k runs before the re-sort, on the
-// touched blocks of the plan its P2G scattered under.
+// due (k a multiple of the cadence), G2P(k) + P2G(k+1); then grid update(n-1) and G2P(n-1).  The
+// state after every substep is in buffer a or b as in the unfused loop (x, F, Jp, ids, per-particle
+// material), with v and C written by the last G2P only.  The grid update of substep k runs before
+// the re-sort, on the touched blocks of the plan its P2G scattered under.  The re-sorts are
+// scheduled on the host: the fused kernel adds the blocks a fast particle reaches to the touched
+// list itself, so correctness does not wait for a re-sort, and substeps without one launch no
+// sort or plan kernel at all.  Keys and the block histogram are written only by the fused launch
+// that precedes a re-sort.
 template <int DIM, typename T>
 int op_substeps_fused(const ffmpm_params& p, const Layout& L, const Ws& w, PView<T> va, PView<T> vb, int32_t* ids_a,
                       int32_t* ids_b, int nsteps, cudaStream_t s, PhaseTimer* tm) {
   const int K = sort_every(p);
-  const uint32_t* flag = &w.hdr->sort_now;
-  const uint32_t* perm = nullptr;
-  k_sort_decide<<<1, 1, 0, s>>>(w.hdr, 1);
-  sort_and_plan<DIM, T>(p, L, w, va, false, &perm, s, tm, flag);
+  const auto resorts = [&](int k) { return k >= 1 && k <= nsteps - 2 && k % K == 0; };
+  const uint32_t* sorted_perm = nullptr;
+  sort_and_plan<DIM, T>(p, L, w, va, false, &sorted_perm, s, tm, nullptr, 1);
+  const uint32_t* perm = sorted_perm;  // the permutation the next P2G / G2P applies (null: none)
   if (tm) tm->begin(3);
-  launch_p2g<DIM, T>(p, L, w, va, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s, flag);
+  launch_p2g<DIM, T>(p, L, w, va, perm, InternalSink<T>{static_cast<Node4<T>*>(w.gridA)}, s);
   if (tm) tm->end(1);
   for (int k = 0; k < nsteps; ++k) {
     const PView<T>& in = (k & 1) ? vb : va;
@@ -428,26 +433,24 @@ int op_substeps_fused(const ffmpm_params& p, const Layout& L, const Ws& w, PView
     launch_grid_update<DIM, T>(p, L, w, s);
     if (tm) tm->end(1);
     if (k == nsteps - 1) {
-      // the buffer holds the order of the current plan: G2P must not apply the last permutation again
-      if (k > 0) cudaMemsetAsync(&w.hdr->sort_now, 0, sizeof(uint32_t), s);
-      G2PExtra ex{ids_in, ids_out, w.keys_next, w.block_count, L.cell_bits, w.gridB, nullptr, 0};
+      // k >= 1: the buffer is already in the order of the current plan
+      G2PExtra ex{ids_in, ids_out, nullptr, nullptr, L.cell_bits, w.gridB, nullptr};
       if (tm) tm->begin(5);
-      const int rc = launch_g2p<DIM, T, true, true>(p, L, w, in, out, perm, nullptr, ex, s, flag);
+      const int rc = launch_g2p<DIM, T, true, true>(p, L, w, in, out, nullptr, nullptr, ex, s);
       if (tm) tm->end(1);
       if (rc != FFMPM_OK) return rc;
       break;
     }
-    if (k > 0) {
-      k_sort_decide<<<1, 1, 0, s>>>(w.hdr, k % K == 0 ? 1 : 0);
-      sort_and_plan<DIM, T>(p, L, w, in, true, &perm, s, tm, flag);
-    }
-    G2PExtra ex{ids_in, ids_out, w.keys_next, w.block_count, L.cell_bits, w.gridB, &w.hdr->far_stray, 1};
+    if (k > 0) perm = nullptr;
+    if (resorts(k)) sort_and_plan<DIM, T>(p, L, w, in, true, &perm, s, tm, nullptr, 1);
+    const bool keys = resorts(k + 1);
+    G2PExtra ex{ids_in, ids_out, keys ? w.keys_next : nullptr, keys ? w.block_count : nullptr, L.cell_bits, w.gridB,
+                nullptr};
     if (tm) tm->begin(6);
-    const int rc = launch_g2p2g<DIM, T>(p, L, w, in, out, perm, ex, s, flag);
+    const int rc = launch_g2p2g<DIM, T>(p, L, w, in, out, perm, ex, s, nullptr);
     if (tm) tm->end(1);
     if (rc != FFMPM_OK) return rc;
   }
-  cudaMemsetAsync(w.block_count, 0, sizeof(uint32_t) * L.nblocks, s);
   return check_launch();
 }
 
@@ -479,7 +482,7 @@ int op_substeps_sorted(const ffmpm_params& p, const Layout& L, const Ws& w, ffmp
       launch_grid_update<DIM, T>(p, L, w, s);
     if (tm) tm->end(1);
     G2PExtra ex{ids_in, ids_out, w.keys_next, w.block_count, L.cell_bits, flag ? w.gridB : nullptr,
-                flag ? &w.hdr->far_stray : nullptr, 0};
+                flag ? &w.hdr->far_stray : nullptr};
     if (tm) tm->begin(5);
     int rc = launch_g2p<DIM, T, true, true>(p, L, w, in, out, perm, nullptr, ex, s, flag);
     if (tm) tm->end(1);
@@ -715,9 +718,9 @@ int ffmpm_kernels_per_call(const ffmpm_params* p, int64_t n, int32_t nsteps, int
   if (n == 0 || nsteps == 0) {
     *count = 0;
   } else if (fused(*p, nsteps)) {
-    // decide + keys + sort + P2G; per substep k < n-1: grid update (+ decide + sort for k > 0) +
-    // fused kernel; the last substep: grid update + G2P
-    *count = (1 + 1 + sort + 1) + 2 + int64_t(nsteps - 2) * (1 + 1 + sort + 1) + 2;
+    // keys + sort + P2G; per substep k < n-1: grid update + fused kernel (+ sort when 1 <= k <= n-2
+    // is a multiple of the cadence); the last substep: grid update + G2P
+    *count = (1 + sort + 1) + int64_t(nsteps - 1) * 2 + int64_t((nsteps - 2) / sort_every(*p)) * sort + 2;
   } else {
     // per substep: (decide) + sort + P2G + grid update + G2P; keys once
     *count = int64_t(nsteps) * ((sort_every(*p) > 1 ? 1 : 0) + sort + 3) + 1;

@@ -1451,10 +1451,6 @@ struct G2PExtra {
   // +-1 of that block (the next substep must then re-sort)
   const void* grid_global;
   uint32_t* far_flag;
-  // cells by which the far test is tightened: 1 when the next scatter of the same particle happens
-  // before the next re-sort can take effect (fused G2P + P2G), so that a particle moving less than a
-  // cell per substep never needs the touched-block fix-up
-  int far_margin;
 };
 
 // The state G2P reads of one particle (loaded ahead of the arithmetic so that the loads of
@@ -1704,7 +1700,7 @@ __device__ __forceinline__ bool g2p_particle(const KParams<T>& kp, const Geom<DI
           T fn;
           base_of(xn[d], kp.inv_dx, kp.res, bn, fn);
           const int l = bn - org[d];
-          far = far || l < -g.bs + ex.far_margin || l > 2 * g.bs - 3 - ex.far_margin;
+          far = far || l < -g.bs || l > 2 * g.bs - 3;
         }
         if (far) *ex.far_flag = 1u;
       }

@@ -137,8 +137,9 @@ def _fast_cluster(dim, n_, res, dt, cells_per_substep):
 def test_cluster_at_the_velocity_clamp(dtype):
     """A 3D cluster launched at 2.5 cells per substep: the grid clamps every node velocity to
     0.9 dx / dt (three_d/grid_op.py:25), so it crosses ~11 cells in 12 substeps with no scheduled
-    re-sort.  Only the far flags (raised a cell early in the fused G2P + P2G) re-sort it.  The
-    result equals the in-place substeps."""
+    re-sort: its particles leave their chunk blocks' tiles (direct global adds and gathers) and
+    then the blocks the plan touches (the fused kernel adds those blocks to the touched list).
+    The result equals the in-place substeps."""
     n_, res, dt, g, steps = 3000, 64, 2e-4, -9.8, 12
     x, v, vol, mu, lam = _fast_cluster(3, n_, res, dt, 2.5)
     solver = MPMSolver(torch.tensor(x), res=res, dt=dt, gravity=g, volume=vol, mass=vol, mu_0=mu, lambda_0=lam,
@@ -160,9 +161,9 @@ def test_cluster_at_the_velocity_clamp(dtype):
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_2d_cluster_faster_than_two_cells_per_substep(dtype):
     """A 2D cluster at 2.5 cells per substep (the 2D grid rule has no velocity clamp,
-    two_d/grid_op.py): in the fused G2P + P2G a particle's new stencil leaves the blocks its plan
-    touches before the re-sort its far flag asks for takes effect, so the kernel adds those blocks
-    to the touched list itself.  Positions and velocities equal the in-place substeps."""
+    two_d/grid_op.py) with no scheduled re-sort: its particles leave the blocks their plan touches
+    within a few substeps, and the fused kernel adds the blocks they reach to the touched list.
+    Positions and velocities equal the in-place substeps."""
     from femflow_gb300.solvers.mpm import two_d
 
     n_, res, dt, g, steps = 3000, 64, 2e-4, -9.8, 12

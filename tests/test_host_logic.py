@@ -69,9 +69,10 @@ def test_kernels_per_call():
     N.call("ffmpm_plan_info", ctypes.byref(E.make_params(3, 128, torch.float32, 1 / 128, 128.0, 1e-4)), 1 << 20, info)
     sort = 1 + info[4] + 1  # digit histogram, radix passes, plan
     every8 = 8 << 8
-    # fused: (decide, keys, sort, P2G) + 2 + (n - 2) (grid, decide, sort, fused) + (grid, G2P)
-    assert count(10, variant=every8) == (3 + sort) + 2 + 8 * (3 + sort) + 2
-    assert count(2, variant=every8) == (3 + sort) + 4
+    # fused: (keys, sort, P2G) + (n - 1) (grid, fused) + the re-sorts at k = 8 + (grid, G2P)
+    assert count(10, variant=every8) == (2 + sort) + 9 * 2 + 1 * sort + 2
+    assert count(2, variant=every8) == (2 + sort) + 2 + 2
+    assert count(20, variant=every8) == (2 + sort) + 19 * 2 + 2 * sort + 2
     # one substep and variant 4: decide, sort, P2G, grid, G2P per substep, keys once
     assert count(1, variant=every8) == 1 + sort + 3 + 1
     assert count(10, variant=every8 | 4) == 10 * (1 + sort + 3) + 1
