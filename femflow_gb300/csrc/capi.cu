@@ -146,6 +146,7 @@ Geom<DIM> geom(const Layout& L) {
   g.res = L.res;
   g.R = L.R;
   g.bs = L.bs;
+  g.bs_shift = __builtin_ctz((unsigned)L.bs);
   g.nb = L.nb;
   g.nblocks = (int)L.nblocks;
   g.tile = L.tile;

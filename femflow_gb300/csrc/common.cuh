@@ -58,7 +58,8 @@ template <int DIM>
 struct Geom {
   int res;     // grid resolution
   int R;       // nodes per axis
-  int bs;      // block side (nodes)
+  int bs;      // block side (nodes), a power of two
+  int bs_shift;  // log2(bs): cell coordinates are decoded with shifts and masks, not divisions
   int nb;      // blocks per axis = ceil(R / bs)
   int nblocks; // nb^DIM
   int tile;    // bs + 2

@@ -119,8 +119,8 @@ __device__ __forceinline__ bool particle_key(const T* xp, const KParams<T>& kp, 
   uint32_t bid = 0, cell = 0;
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
-    bid = bid * g.nb + (uint32_t)(b[d] / g.bs);
-    cell = cell * g.bs + (uint32_t)(b[d] % g.bs);
+    bid = bid * g.nb + (uint32_t)(b[d] >> g.bs_shift);
+    cell = (cell << g.bs_shift) | (uint32_t)(b[d] & (g.bs - 1));
   }
   blk = bid;
   key = cell_bits ? ((bid << cell_bits) | cell) : bid;
@@ -153,6 +153,8 @@ __global__ void __launch_bounds__(kThreads) k_keys(KParams<T> kp, Geom<DIM> g, P
 struct Scan4 {
   uint32_t a, b, c, d;
 };
+
+constexpr int kPlanBitmapWords = 5632;  // 22 KB of shared memory per bitmap: grids of up to 180,224 blocks
 
 __device__ __forceinline__ Scan4 block_exclusive_scan4(Scan4 v, Scan4* total, Scan4* warp_buf) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -199,6 +201,51 @@ __global__ void __launch_bounds__(1024) k_plan(Geom<DIM> g, uint32_t* __restrict
     return;
   }
   __shared__ Scan4 warp_buf[32];
+  // Touched blocks as a bitmap: every occupied block sets the bits of the blocks its stencils can
+  // reach (b + {0,1}^DIM, or b + {-1,0,1}^DIM with `sym`), so the work is proportional to the
+  // occupied blocks, not to all blocks times their neighbourhood.  Grids with more blocks than the
+  // bitmap holds test the neighbourhood of every block against the histogram instead.
+  __shared__ uint32_t occ_bits[kPlanBitmapWords];
+  __shared__ uint32_t tch_bits[kPlanBitmapWords];
+  const bool use_bits = g.nblocks <= kPlanBitmapWords * 32;
+  if (use_bits) {
+    const int nwords = (g.nblocks + 31) / 32;
+    for (int wd = threadIdx.x; wd < nwords; wd += blockDim.x) tch_bits[wd] = 0u;
+    for (int wd = threadIdx.x >> 5; wd < nwords; wd += blockDim.x >> 5) {
+      const int b = wd * 32 + (threadIdx.x & 31);
+      const unsigned m = __ballot_sync(0xffffffffu, b < g.nblocks && block_count[b] > 0);
+      if ((threadIdx.x & 31) == 0) occ_bits[wd] = m;
+    }
+    __syncthreads();
+    const int NO = sym ? (DIM == 3 ? 27 : 9) : (1 << DIM);
+    for (int b = threadIdx.x; b < g.nblocks; b += blockDim.x) {
+      if (!((occ_bits[b >> 5] >> (b & 31)) & 1u)) continue;
+      int bc[DIM];
+      block_coords<DIM>(g, b, bc);
+      for (int o = 0; o < NO; ++o) {
+        int id = 0, r = o;
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          // offsets of axis d: sym -> (o / 3^(DIM-1-d)) % 3 - 1, else bit DIM-1-d of o
+          int od;
+          if (sym) {
+            int div = 1;
+#pragma unroll
+            for (int e = d + 1; e < DIM; ++e) div *= 3;
+            od = (r / div) % 3 - 1;
+          } else {
+            od = (o >> (DIM - 1 - d)) & 1;
+          }
+          const int cc = bc[d] + od;
+          ok = ok && cc >= 0 && cc < g.nb;
+          id = id * g.nb + cc;
+        }
+        if (ok) atomicOr(&tch_bits[id >> 5], 1u << (id & 31));
+      }
+    }
+    __syncthreads();
+  }
   Scan4 carry{0, 0, 0, 0};  // (particles, chunks, touched, occupied)
   for (int seg = 0; seg < g.nblocks; seg += blockDim.x) {
     const int b = seg + threadIdx.x;
@@ -209,7 +256,9 @@ __global__ void __launch_bounds__(1024) k_plan(Geom<DIM> g, uint32_t* __restrict
       block_coords<DIM>(g, b, bc);
       // touched if any block b - o, o in {0,1}^DIM, holds particles; with `sym` (plans kept over
       // several substeps) any block b + o, o in {-1,0,1}^DIM
-      if (!sym) {
+      if (use_bits) {
+        tch = (tch_bits[b >> 5] >> (b & 31)) & 1u;
+      } else if (!sym) {
 #pragma unroll
         for (int o = 0; o < (1 << DIM); ++o) {
           int nb_id = 0;
@@ -923,15 +972,15 @@ __device__ __forceinline__ void p2g_cell_runs(const CellRunSmem<T>& cr, const Ge
       const int cl = cells[order[l0]];
       int lb[DIM];
       if constexpr (DIM == 3) {
-        lb[2] = cl % g.bs;
-        lb[1] = (cl / g.bs) % g.bs;
-        lb[0] = cl / (g.bs * g.bs);
+        lb[2] = cl & (g.bs - 1);
+        lb[1] = (cl >> g.bs_shift) & (g.bs - 1);
+        lb[0] = cl >> (2 * g.bs_shift);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
           tacc.add(lb[0] + i, lb[1] + oj, lb[2] + ok, acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
       } else {
-        lb[1] = cl % g.bs;
-        lb[0] = cl / g.bs;
+        lb[1] = cl & (g.bs - 1);
+        lb[0] = cl >> g.bs_shift;
 #pragma unroll
         for (int i = 0; i < 3; ++i) tacc.add(lb[0] + i, lb[1] + oj, 0, acc[i][0], acc[i][1], T(0), acc[i][3]);
       }
@@ -1172,12 +1221,12 @@ __global__ void __launch_bounds__(kThreads) k_p2g_det(KParams<T> kp, Geom<DIM> g
         if (grp == 0) {
           int lb[DIM];
           if constexpr (DIM == 3) {
-            lb[2] = cl % g.bs;
-            lb[1] = (cl / g.bs) % g.bs;
-            lb[0] = cl / (g.bs * g.bs);
+            lb[2] = cl & (g.bs - 1);
+            lb[1] = (cl >> g.bs_shift) & (g.bs - 1);
+            lb[0] = cl >> (2 * g.bs_shift);
           } else {
-            lb[1] = cl % g.bs;
-            lb[0] = cl / g.bs;
+            lb[1] = cl & (g.bs - 1);
+            lb[0] = cl >> g.bs_shift;
           }
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
@@ -1319,12 +1368,12 @@ __global__ void __launch_bounds__(kThreads) k_grid_update(KParams<T> kp, Geom<DI
     for (int t = threadIdx.x; t < per_block; t += blockDim.x) {
       int I[DIM];
       if constexpr (DIM == 3) {
-        I[0] = bc[0] * g.bs + t / (g.bs * g.bs);
-        I[1] = bc[1] * g.bs + (t / g.bs) % g.bs;
-        I[2] = bc[2] * g.bs + t % g.bs;
+        I[0] = bc[0] * g.bs + (t >> (2 * g.bs_shift));
+        I[1] = bc[1] * g.bs + ((t >> g.bs_shift) & (g.bs - 1));
+        I[2] = bc[2] * g.bs + (t & (g.bs - 1));
       } else {
-        I[0] = bc[0] * g.bs + t / g.bs;
-        I[1] = bc[1] * g.bs + t % g.bs;
+        I[0] = bc[0] * g.bs + (t >> g.bs_shift);
+        I[1] = bc[1] * g.bs + (t & (g.bs - 1));
       }
       bool in = true;
 #pragma unroll
@@ -1359,12 +1408,12 @@ __global__ void __launch_bounds__(kThreads) k_grid_update_det(KParams<T> kp, Geo
     for (int t = threadIdx.x; t < per_block; t += blockDim.x) {
       int loc[DIM], I[DIM];
       if constexpr (DIM == 3) {
-        loc[0] = t / (g.bs * g.bs);
-        loc[1] = (t / g.bs) % g.bs;
-        loc[2] = t % g.bs;
+        loc[0] = t >> (2 * g.bs_shift);
+        loc[1] = (t >> g.bs_shift) & (g.bs - 1);
+        loc[2] = t & (g.bs - 1);
       } else {
-        loc[0] = t / g.bs;
-        loc[1] = t % g.bs;
+        loc[0] = t >> g.bs_shift;
+        loc[1] = t & (g.bs - 1);
       }
       bool in = true;
 #pragma unroll
@@ -1828,8 +1877,8 @@ __device__ __forceinline__ void mark_touched(const Geom<DIM>& g, const int base[
   int lo[DIM], ext[DIM];
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
-    lo[d] = base[d] / g.bs;
-    ext[d] = min((base[d] + 2) / g.bs, g.nb - 1) - lo[d];  // 0 or 1
+    lo[d] = base[d] >> g.bs_shift;
+    ext[d] = min((base[d] + 2) >> g.bs_shift, g.nb - 1) - lo[d];  // 0 or 1
   }
   for (int o = 0; o < (1 << DIM); ++o) {
     int id = 0;

@@ -53,6 +53,7 @@ void sort_static(const ffmpm_params& p, const Layout& L, uint32_t* base, const v
   g.res = L.res;
   g.R = L.R;
   g.bs = L.bs;
+  g.bs_shift = __builtin_ctz((unsigned)L.bs);
   g.nb = L.nb;
   g.nblocks = (int)L.nblocks;
   g.tile = L.tile;
