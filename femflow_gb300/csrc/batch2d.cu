@@ -212,9 +212,9 @@ __global__ void __launch_bounds__(kBatchMaxThreads) k_batch2d_substep(unsigned c
     const int si = find_scene(s_noff, nscenes, gn);
     const ffmpm_scene2d& sc = s_sc[si];
     const KParams<T> kp = scene_kparams<T>(sc);
-    const int64_t li = gn - s_noff[si];
+    const int li = (int)(gn - s_noff[si]);  // node of the scene: at most 257^2, 32-bit division
     const int R = kp.res + 1;
-    int I[2] = {(int)(li / R), (int)(li % R)};
+    int I[2] = {li / R, li % R};
     const Node4<T> a = A[gn];
     T vel[3] = {a.x, a.y, a.z};
     grid_node<2, T>(kp, I, vel, a.w);
