@@ -127,6 +127,9 @@ class Staged:
     host: list
 
     def write_back(self, indices):
+        """Copy the device arrays back into their host originals; copies into pinned host tensors
+        are queued together and waited for once."""
+        pending = None
         for i in indices:
             h, d = self.host[i], self.dev[i]
             if h is None or d is None:
@@ -134,7 +137,12 @@ class Staged:
             if isinstance(h, np.ndarray):
                 h[...] = d.cpu().numpy().astype(h.dtype, copy=False).reshape(h.shape)
             elif h is not d:
-                h.copy_(d.view(h.shape), non_blocking=False)
+                pinned = h.is_pinned()
+                h.copy_(d.view(h.shape), non_blocking=pinned)
+                if pinned:
+                    pending = d.device
+        if pending is not None:
+            torch.cuda.current_stream(pending).synchronize()
 
 
 def stage(arrays, device=None, dtype=None) -> Staged:
