@@ -43,7 +43,12 @@ class Params(ctypes.Structure):
         ("dx", ctypes.c_double), ("inv_dx", ctypes.c_double), ("dt", ctypes.c_double), ("gravity", ctypes.c_double),
         ("volume", ctypes.c_double), ("hardening", ctypes.c_double), ("mass", ctypes.c_double),
         ("mu_0", ctypes.c_double), ("lambda_0", ctypes.c_double),
+        ("n_planes", ctypes.c_int32), ("plane_rule", ctypes.c_int32), ("planes", (ctypes.c_double * 6) * 8),
     ]
+
+
+MAX_PLANES = 8
+PLANE_RULES = {"sticky": 0, "reference_literal": 1}
 
 
 class Particles(ctypes.Structure):
@@ -96,6 +101,8 @@ _PROTOS = {
     "ffmpm_diagnostics_fp64": (ctypes.c_int, [_P(Params), _P(Particles), _vp, _vp]),
     "ffmpm_profile_substeps": (ctypes.c_int, [_P(Params), _P(Particles), _P(Particles), _vp, _vp, ctypes.c_int32,
                                               _vp, ctypes.c_size_t, _vp, _P(ctypes.c_double), _P(ctypes.c_int64)]),
+    "ffmpm_check_collision_points": (ctypes.c_int, [_P(Params), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                                     ctypes.c_void_p, ctypes.c_void_p]),
     "ffmpm_plan_info": (ctypes.c_int, [_P(Params), ctypes.c_int64, _P(ctypes.c_int64)]),
     "ffmpm_kernels_per_call": (ctypes.c_int, [_P(Params), ctypes.c_int64, ctypes.c_int32, _P(ctypes.c_int64)]),
     "ffmpm_sort_by_block_static": (ctypes.c_int, [_P(Params), _vp, ctypes.c_int64, _vp, _vp, _vp]),

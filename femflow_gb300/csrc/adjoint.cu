@@ -256,6 +256,9 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_grid(KParams<double> kp, co
     for (int d = 0; d < 3; ++d) near = near || I[d] < 3 || I[d] > kp.res - 3;
     if (near) vb[0] = vb[1] = vb[2] = T(0);
   }
+  // planar colliders zero the node velocity: nothing passes back through them
+  for (int q = 0; q < kp.n_planes; ++q)
+    if (behind_plane<3, double>(kp, I, q)) vb[0] = vb[1] = vb[2] = T(0);
   Node4<double> o;
   if (m > T(0)) {
     const T im = T(1) / m;

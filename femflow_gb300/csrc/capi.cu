@@ -42,6 +42,15 @@ bool valid_params(const ffmpm_params* p) {
   if (p->wall_mode != FFMPM_WALLS_REFERENCE && p->wall_mode != FFMPM_WALLS_STICKY3) return false;
   if (p->block_size != 0 && (p->block_size < 2 || p->block_size > 16 || (p->block_size & (p->block_size - 1))))
     return false;
+  if (p->n_planes < 0 || p->n_planes > FFMPM_MAX_PLANES) return false;
+  if (p->plane_rule != FFMPM_PLANES_STICKY && p->plane_rule != FFMPM_PLANES_REFERENCE_LITERAL) return false;
+  for (int q = 0; q < p->n_planes; ++q) {
+    double ss = 0.0;
+    for (int d = 0; d < 6; ++d)
+      if (!std::isfinite(p->planes[q][d])) return false;
+    for (int d = 0; d < p->dim; ++d) ss += p->planes[q][3 + d] * p->planes[q][3 + d];
+    if (!(ss > 0.0)) return false;
+  }
   return true;
 }
 
@@ -710,6 +719,48 @@ int ffmpm_plan_info(const ffmpm_params* p, int64_t n, int64_t* info) {
   info[6] = L.tile;
   info[7] = L.max_chunks;
   return FFMPM_OK;
+}
+
+int ffmpm_check_collision_points(const ffmpm_params* p, const double* points, const double* normals, int32_t n,
+                                 void* grid_velocity, void* stream) {
+  if (!p || n < 0 || (n > 0 && (!points || !normals || !grid_velocity))) return FFMPM_ERR_BADARG;
+  if (!valid_params(p)) return FFMPM_ERR_BADARG;
+  if (p->plane_rule != FFMPM_PLANES_STICKY && p->plane_rule != FFMPM_PLANES_REFERENCE_LITERAL) return FFMPM_ERR_BADARG;
+  const int dim = p->dim;
+  for (int i = 0; i < n * dim; ++i)
+    if (!std::isfinite(points[i]) || !std::isfinite(normals[i])) return FFMPM_ERR_BADARG;
+  for (int i = 0; i < n; ++i) {
+    double ss = 0.0;
+    for (int d = 0; d < dim; ++d) ss += normals[i * dim + d] * normals[i * dim + d];
+    if (!(ss > 0.0)) return FFMPM_ERR_BADARG;  // the reference divides by |normal|
+  }
+  const int64_t R = p->res + 1;
+  const int64_t nnodes = dim == 3 ? R * R * R : R * R;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // the planes go to the kernel in batches of FFMPM_MAX_PLANES (zeroing is idempotent, so the
+  // batches compose like the reference's loop over planes)
+  for (int b = 0; b < n; b += FFMPM_MAX_PLANES) {
+    ffmpm_params q = *p;
+    q.n_planes = std::min(n - b, FFMPM_MAX_PLANES);
+    for (int i = 0; i < q.n_planes; ++i)
+      for (int d = 0; d < 3; ++d) {
+        q.planes[i][d] = d < dim ? points[(b + i) * dim + d] : 0.0;
+        q.planes[i][3 + d] = d < dim ? normals[(b + i) * dim + d] : 0.0;
+      }
+    const int blocks = work_grid((nnodes + kThreads - 1) / kThreads, 8);
+    if (p->real_bytes == 4) {
+      if (dim == 3)
+        k_collision_points<3, float><<<blocks, kThreads, 0, s>>>(kparams<float>(q), static_cast<float*>(grid_velocity), nnodes);
+      else
+        k_collision_points<2, float><<<blocks, kThreads, 0, s>>>(kparams<float>(q), static_cast<float*>(grid_velocity), nnodes);
+    } else {
+      if (dim == 3)
+        k_collision_points<3, double><<<blocks, kThreads, 0, s>>>(kparams<double>(q), static_cast<double*>(grid_velocity), nnodes);
+      else
+        k_collision_points<2, double><<<blocks, kThreads, 0, s>>>(kparams<double>(q), static_cast<double*>(grid_velocity), nnodes);
+    }
+  }
+  return check_launch();
 }
 
 int ffmpm_kernels_per_call(const ffmpm_params* p, int64_t n, int32_t nsteps, int64_t* count) {

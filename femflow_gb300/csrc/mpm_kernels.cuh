@@ -12,6 +12,8 @@
 //                                                            (three_d/g2p.py:9-59)
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -24,7 +26,34 @@ template <typename T>
 struct KParams {
   T dx, inv_dx, dt, gravity, volume, hardening, mass, mu0, lam0, v_allowed;
   int res, model, wall_mode, variant;
+  // planar colliders: {point, normal'} in float64 with the plane rule already applied to the normal
+  int n_planes = 0;
+  double dx64 = 0.0;
+  double planes[FFMPM_MAX_PLANES][6] = {};
 };
+
+// normal' of plane q of the params under the plane rule (three_d/grid_op.py:59-60)
+inline void plane_normal(const ffmpm_params& p, int q, double out[3]) {
+  const double* nr = p.planes[q] + 3;
+  const int dim = p.dim;
+  double ss = 0.0;
+  for (int d = 0; d < dim; ++d) ss += nr[d] * nr[d];
+  const double add = p.plane_rule == FFMPM_PLANES_REFERENCE_LITERAL ? 1.0 / std::sqrt(ss) : 0.0;
+  for (int d = 0; d < 3; ++d) out[d] = d < dim ? nr[d] + add : 0.0;
+}
+
+// True when node I lies strictly on the negative side of plane q: (I dx - point) . normal' < 0,
+// products and sums rounded one at a time in float64 as numpy computes them.
+template <int DIM, typename T>
+__device__ __forceinline__ bool behind_plane(const KParams<T>& kp, const int I[DIM], int q) {
+  double dot = 0.0;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    const double off = __dsub_rn(__dmul_rn(double(I[d]), kp.dx64), kp.planes[q][d]);
+    dot = __dadd_rn(dot, __dmul_rn(off, kp.planes[q][3 + d]));
+  }
+  return dot < 0.0;
+}
 
 // Variant flags (ffmpm_params.variant).
 constexpr int kVariantP2GDirect = 1;  // P2G scatters straight to L2 with vector reds (no smem tile)
@@ -61,6 +90,16 @@ inline KParams<T> kparams(const ffmpm_params& p) {
   k.model = p.model;
   k.wall_mode = p.wall_mode;
   k.variant = p.variant;
+  k.n_planes = std::max(0, std::min(int(p.n_planes), FFMPM_MAX_PLANES));
+  k.dx64 = p.dx;
+  for (int q = 0; q < k.n_planes; ++q) {
+    double nrm[3];
+    plane_normal(p, q, nrm);
+    for (int d = 0; d < 3; ++d) {
+      k.planes[q][d] = d < p.dim ? p.planes[q][d] : 0.0;
+      k.planes[q][3 + d] = nrm[d];
+    }
+  }
   return k;
 }
 
@@ -1353,6 +1392,9 @@ __device__ __forceinline__ void grid_node(const KParams<T>& kp, const int I[DIM]
     }
     vel[2] = T(0);
   }
+  // planar colliders (sticky), after the walls
+  for (int q = 0; q < kp.n_planes; ++q)
+    if (behind_plane<DIM, T>(kp, I, q)) vel[0] = vel[1] = vel[2] = T(0);
 }
 
 template <int DIM, typename T>
@@ -1999,6 +2041,32 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_g2p2g(
   if (cur >= 0) {
     __syncthreads();
     p2g_flush<DIM, T, InternalSink<T>>(ptile, TN, g, org, sink);
+  }
+}
+
+// ----------------------------------------------------------------------------------------------
+// three_d/grid_op.py:50-67 check_collision_points on a caller's dense grid velocity
+// [(res+1)^DIM][DIM]: every node behind one of the params' planes gets velocity zero.
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kThreads) k_collision_points(KParams<T> kp, T* __restrict__ gv, int64_t nnodes) {
+  const int R = kp.res + 1;
+  for (int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; node < nnodes;
+       node += (int64_t)gridDim.x * blockDim.x) {
+    int I[DIM];
+    if constexpr (DIM == 3) {
+      I[0] = (int)(node / ((int64_t)R * R));
+      I[1] = (int)((node / R) % R);
+      I[2] = (int)(node % R);
+    } else {
+      I[0] = (int)(node / R);
+      I[1] = (int)(node % R);
+    }
+    bool hit = false;
+    for (int q = 0; q < kp.n_planes; ++q) hit = hit || behind_plane<DIM, T>(kp, I, q);
+    if (hit) {
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) gv[node * DIM + d] = T(0);
+    }
   }
 }
 

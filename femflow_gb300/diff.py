@@ -40,6 +40,9 @@ class RolloutConfig:
     # "neo_hookean": the reference's stress (lam(J-1)J on all nine entries of PF, utils.py:129);
     # "fixed_corotated": the textbook fixed-corotated stress (lam(J-1)J on the diagonal only)
     model: str = "neo_hookean"
+    # planar colliders ((point, normal) pairs) applied by every grid update, and their rule
+    planes: tuple = ()
+    plane_rule: str = "sticky"
 
 
 def lame(E_mod, nu):
@@ -71,7 +74,8 @@ class _Runner:
         self.dtype = dtype
         self.device = device
         self.params = E.make_params(3, cfg.res, dtype, 1.0 / cfg.res, float(cfg.res), cfg.dt, cfg.gravity,
-                                    cfg.volume, cfg.hardening, model=cfg.model, wall_mode=cfg.wall_mode)
+                                    cfg.volume, cfg.hardening, model=cfg.model, wall_mode=cfg.wall_mode,
+                                    planes=cfg.planes, plane_rule=cfg.plane_rule)
         if torch.is_tensor(mass):
             self.mass = mass.detach().to(device=device, dtype=dtype).reshape(n).contiguous()
         else:

@@ -37,7 +37,10 @@ def real_bytes(dtype) -> int:
 def make_params(dim: int, res: int, dtype, dx: float, inv_dx: float, dt: float, gravity: float = 0.0,
                 volume: float = 1.0, hardening: float = 1.0, mass: float = 0.0, mu_0: float = 0.0,
                 lambda_0: float = 0.0, model="neo_hookean", wall_mode="reference", deterministic: bool = False,
-                block_size: int = 0, variant: int = 0) -> N.Params:
+                block_size: int = 0, variant: int = 0, planes=None, plane_rule="sticky") -> N.Params:
+    """Kernel parameters.  ``planes``: up to 8 planar colliders as (point, normal) pairs of ``dim``
+    numbers each, applied by every grid update (``plane_rule`` "sticky" or "reference_literal",
+    see ffmpm_params in include/femflow_mpm.h)."""
     p = N.Params()
     p.dim, p.res, p.real_bytes = int(dim), int(res), real_bytes(dtype)
     p.model = N.MODELS[model] if isinstance(model, str) else int(model)
@@ -46,6 +49,17 @@ def make_params(dim: int, res: int, dtype, dx: float, inv_dx: float, dt: float, 
     p.dx, p.inv_dx, p.dt, p.gravity = float(dx), float(inv_dx), float(dt), float(gravity)
     p.volume, p.hardening = float(volume), float(hardening)
     p.mass, p.mu_0, p.lambda_0 = float(mass), float(mu_0), float(lambda_0)
+    planes = list(planes or [])
+    if len(planes) > N.MAX_PLANES:
+        raise ValueError(f"at most {N.MAX_PLANES} planes")
+    p.n_planes = len(planes)
+    p.plane_rule = N.PLANE_RULES[plane_rule] if isinstance(plane_rule, str) else int(plane_rule)
+    for q, (point, normal) in enumerate(planes):
+        point, normal = np.asarray(point, dtype=np.float64), np.asarray(normal, dtype=np.float64)
+        if point.shape != (dim,) or normal.shape != (dim,):
+            raise ValueError(f"a plane is a point and a normal of {dim} numbers each")
+        for d in range(dim):
+            p.planes[q][d], p.planes[q][3 + d] = float(point[d]), float(normal[d])
     return p
 
 

@@ -50,14 +50,17 @@ class MPMSolver:
     Args mirror ``solve_mls_mpm_3d`` (mls_mpm.py:40-53) plus the 2D scalars of two_d.p2g:
     ``dim``, ``res``, ``dt``, ``gravity``, ``volume``, ``hardening``; material either per particle
     (``mass``, ``mu_0``, ``lambda_0`` tensors) or scalar.  ``sort_every``: substeps between re-sorts
-    by block (a particle that leaves the blocks around its own before then triggers an earlier one;
-    the deterministic mode re-sorts every substep).
+    by block (with separate G2P and P2G launches a particle that leaves the blocks around its own
+    triggers an earlier one; the fused path handles such particles in place; the deterministic mode
+    re-sorts every substep).  ``planes``: up to 8 planar colliders (point, normal) that every grid
+    update applies (three_d/grid_op.py:50-67; ``plane_rule`` "sticky" or "reference_literal").
     """
 
     def __init__(self, x, *, res: int, dt: float, gravity: float = -9.8, volume: float = 1.0,
                  hardening: float = 1.0, mass=1.0, mu_0=0.0, lambda_0=0.0, v=None, F=None, C=None, Jp=None,
                  dtype=torch.float32, device="cuda", model="neo_hookean", wall_mode="reference",
-                 block_size: int = 0, variant: int = 0, deterministic: bool = False, sort_every: int = 8):
+                 block_size: int = 0, variant: int = 0, deterministic: bool = False, sort_every: int = 8,
+                 planes=None, plane_rule: str = "sticky"):
         E._require_cuda()
         device = torch.device(device)
         x = torch.as_tensor(x)
@@ -70,7 +73,7 @@ class MPMSolver:
                                     0.0 if per_particle else float(lambda_0), model=model, wall_mode=wall_mode,
                                     block_size=block_size,
                                     variant=(variant & 0xFF) | (max(1, min(255, int(sort_every))) << 8),
-                                    deterministic=deterministic)
+                                    deterministic=deterministic, planes=planes, plane_rule=plane_rule)
         self._a = _Buffers(n, dim, dtype, device, per_particle)
         self._b = _Buffers(n, dim, dtype, device, per_particle)
         a = self._a

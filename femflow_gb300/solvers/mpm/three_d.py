@@ -8,6 +8,9 @@ from __future__ import annotations
 
 import ctypes
 
+import numpy as np
+import torch
+
 from ... import _native as N
 from ... import engine as E
 from . import _phase as P
@@ -60,3 +63,29 @@ def g2p(inv_dx, dt, grid_velocity, particles, v, F, C, Jp, model: str = "neo_hoo
     st.write_back([0, 1, 2, 3, 4])
     if plist is not None:
         pset.write_positions(plist)
+
+
+def check_collision_points(points, normals, grid_resolution, dx, grid_velocity, rule: str = "reference_literal"):
+    """three_d/grid_op.py:50-67: for every plane (point, normal) and every grid node I, zero the
+    node's velocity where (I dx - point) . normal' < 0, in place on the caller's grid.
+
+    ``rule="reference_literal"`` (default, the reference's behaviour) uses normal' = normal +
+    1/|normal| exactly as line 60 writes it, which tilts the plane; ``rule="sticky"`` uses the
+    normal itself (what normalising would give, the evident intent).  The solvers take planes
+    through ``planes=`` instead and apply them inside every grid update.
+    """
+    points = np.asarray(points.cpu() if isinstance(points, torch.Tensor) else points, dtype=np.float64).reshape(-1, 3)
+    normals = np.asarray(normals.cpu() if isinstance(normals, torch.Tensor) else normals,
+                         dtype=np.float64).reshape(-1, 3)
+    if points.shape != normals.shape:
+        raise ValueError("points and normals differ in length")
+    dtype = P.dtype_of(grid_velocity)
+    st = E.stage([grid_velocity], dtype=dtype)
+    (gv,) = st.dev
+    E.check_tensors(dtype, gv)
+    prm = E.make_params(3, grid_resolution, dtype, dx, 1.0 / dx, 1.0, plane_rule=rule)
+    pts = np.ascontiguousarray(points)
+    nrm = np.ascontiguousarray(normals)
+    N.call("ffmpm_check_collision_points", ctypes.byref(prm), pts.ctypes.data_as(ctypes.c_void_p),
+           nrm.ctypes.data_as(ctypes.c_void_p), int(len(pts)), ctypes.c_void_p(gv.data_ptr()), P.stream(gv.device))
+    st.write_back([0])

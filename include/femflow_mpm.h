@@ -57,6 +57,10 @@ extern "C" {
 #define FFMPM_WALLS_REFERENCE 0 /* 3D: three_d/grid_op.py:38-47;  2D: two_d/grid_op.py:13-24 */
 #define FFMPM_WALLS_STICKY3 1   /* all velocity zeroed within 3 cells of every face */
 
+#define FFMPM_MAX_PLANES 8
+#define FFMPM_PLANES_STICKY 0
+#define FFMPM_PLANES_REFERENCE_LITERAL 1
+
 typedef struct ffmpm_params {
   int32_t dim;          /* 2 or 3 */
   int32_t res;          /* grid resolution; nodes per axis = res + 1 */
@@ -71,6 +75,15 @@ typedef struct ffmpm_params {
   double volume;        /* particle volume (reference argument `volume`) */
   double hardening;     /* reference argument `hardening` */
   double mass, mu_0, lambda_0; /* scalar material used when the per-particle pointers are NULL */
+  /* Planar colliders applied by the grid update after the walls (three_d/grid_op.py:50-67
+   * check_collision_points, which the reference defines but never calls): a node I with
+   * (I dx - point) . normal' < 0 has its velocity set to zero (sticky).  plane_rule picks normal':
+   * FFMPM_PLANES_STICKY = the given normal (the reference's evident intent: normalising does not
+   * change the sign), FFMPM_PLANES_REFERENCE_LITERAL = normal + 1/|normal| as the reference's line
+   * :60 writes it.  planes[i] = {point x, y, z, normal x, y, z} (z ignored in 2D). */
+  int32_t n_planes;     /* 0..FFMPM_MAX_PLANES */
+  int32_t plane_rule;   /* FFMPM_PLANES_* */
+  double planes[FFMPM_MAX_PLANES][6];
 } ffmpm_params;
 
 typedef struct ffmpm_particles {
@@ -87,6 +100,14 @@ typedef struct ffmpm_grid {
   void *velocity; /* [(res+1)^dim][dim] */
   void *mass;     /* [(res+1)^dim] */
 } ffmpm_grid;
+
+/* three_d.check_collision_points (three_d/grid_op.py:50-67) on the caller's dense grid velocity
+ * [(res+1)^dim][dim] (real type p->real_bytes): for each of the n planes (points[i], normals[i],
+ * host arrays of dim doubles each) and every node I, zero the node's velocity where
+ * (I dx - point) . normal' < 0, normal' as p->plane_rule says (the planes in p are not used).
+ * Asynchronous on `stream`; no workspace. */
+int ffmpm_check_collision_points(const ffmpm_params *p, const double *points, const double *normals, int32_t n,
+                                 void *grid_velocity, void *stream);
 
 /* Bytes of workspace needed for `n` particles with these params. */
 int ffmpm_workspace_size(const ffmpm_params *p, int64_t n, size_t *bytes);

@@ -21,6 +21,10 @@ Fixtures written:
   ref2d_*.npz     seeded 2D cases run through two_d.p2g / grid_op / g2p.
   ref3d_*.npz     seeded 3D cases run through three_d.p2g / grid_op / g2p and solve_mls_mpm_3d.
   primitives.npz  lattice and scene points of femflow/simulation/mpm/primitives.py.
+  colliders.npz   three_d/grid_op.py:50-67 check_collision_points (defined, never called by the
+                  reference) on seeded grids and planes, including its literal normal + 1/|normal|.
+
+``--only colliders`` regenerates that fixture alone.
 """
 from __future__ import annotations
 
@@ -226,9 +230,37 @@ def make_primitives(ref_root):
     np.savez_compressed(os.path.join(HERE, "primitives.npz"), **out)
 
 
+def make_colliders(ref):
+    """check_collision_points on two seeded 13^3 grids with three seeded planes each."""
+    import importlib
+
+    # the module (three_d/__init__.py re-exports the grid_op function under the same name)
+    ref_grid_op = importlib.import_module("femflow.solvers.mpm.three_d.grid_op")
+
+    out = {}
+    for case, seed in (("a", 0), ("b", 1)):
+        rng = np.random.default_rng(100 + seed)
+        res, dx = 12, 1.0 / 12
+        gv = rng.normal(0.0, 1.0, (res + 1, res + 1, res + 1, 3))
+        points = rng.uniform(0.2, 0.8, (3, 3))
+        normals = rng.normal(0.0, 1.0, (3, 3))
+        got = gv.copy()
+        ref_grid_op.check_collision_points(points, normals, res, dx, got)
+        out.update({f"{case}_res": res, f"{case}_dx": dx, f"{case}_points": points, f"{case}_normals": normals,
+                    f"{case}_grid_in": gv, f"{case}_grid_out": got})
+    np.savez_compressed(os.path.join(HERE, "colliders.npz"), **out)
+
+
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    ref_root = args[0] if args else "/root/reference"
     ref = install_reference(ref_root)
+    if "--only" in sys.argv:
+        only = sys.argv[sys.argv.index("--only") + 1]
+        {"colliders": lambda: make_colliders(ref)}[only]()
+        print(f"{only} fixture written to", HERE)
+        return
+    make_colliders(ref)
     make_primitives(ref_root)
     make_kat(ref, ref_root)
     # C1-like scene (block in [0.3,0.6]x[0.4,0.7], rho=1, E=1e4, nu=0.2) at reduced N/res.

@@ -156,3 +156,32 @@ def test_oracle_snow_3d_clamps_singular_values():
     # Jp absorbs the clamped volume change: Jp * det(F) is the unclamped det (grid velocity 0 here)
     Fin = np.array([np.diag(d) for d in np.diagonal(F, axis1=1, axis2=2)])
     assert np.all((Jp[:, 0] >= 0.6) & (Jp[:, 0] <= 20.0))
+
+
+def test_collider_oracle_matches_reference_fixture():
+    """oracle/colliders.py against the reference's own check_collision_points (grid_op.py:50-67,
+    run unmodified by tests/golden/make_golden.py) on two seeded 13^3 grids with three planes."""
+    import os
+
+    from oracle import colliders as OC
+
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "colliders.npz"))
+    for c in "ab":
+        got = d[f"{c}_grid_in"].copy()
+        OC.check_collision_points(d[f"{c}_points"], d[f"{c}_normals"], int(d[f"{c}_res"]), float(d[f"{c}_dx"]), got)
+        assert np.array_equal(got, d[f"{c}_grid_out"])
+
+
+def test_collider_rules_known_answer():
+    """Plane through y = 0.5 with normal +y: "sticky" zeroes exactly the nodes with y < 0.5; the
+    reference's literal normal' = normal + 1/|normal| = (1, 2, 1) tilts the plane."""
+    from oracle import colliders as OC
+
+    res, dx = 8, 1 / 8
+    R = res + 1
+    I = np.stack(np.unravel_index(np.arange(R ** 3), (R, R, R)), axis=1)
+    m_sticky, _ = OC.behind([[0.0, 0.5, 0.0]], [[0.0, 1.0, 0.0]], res, dx, 3, "sticky")
+    assert np.array_equal(m_sticky, I[:, 1] * dx < 0.5)
+    m_lit, _ = OC.behind([[0.0, 0.5, 0.0]], [[0.0, 1.0, 0.0]], res, dx, 3, "reference_literal")
+    assert np.array_equal(m_lit, I[:, 0] * dx + 2 * (I[:, 1] * dx - 0.5) + I[:, 2] * dx < 0)
+    assert (m_lit != m_sticky).any()
