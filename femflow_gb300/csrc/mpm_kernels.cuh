@@ -410,31 +410,40 @@ __device__ __forceinline__ bool f_minus_r_small_strain3(const T F[9], T FmR[9]) 
   T H[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) H[i] = F[i] - (i % 4 == 0 ? T(1) : T(0));
+  // E and Y are symmetric (every entry (a, b) is formed exactly like (b, a)), so only the six
+  // entries a <= b are computed and mirrored: bit-identical to the full products
   T E[9], emax = T(0);
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int b = 0; b < 3; ++b) {
+    for (int b = a; b < 3; ++b) {
       const T e = H[a * 3 + b] + H[b * 3 + a] + H[0 * 3 + a] * H[0 * 3 + b] + H[1 * 3 + a] * H[1 * 3 + b] +
                   H[2 * 3 + a] * H[2 * 3 + b];
-      E[a * 3 + b] = e;
+      E[a * 3 + b] = E[b * 3 + a] = e;
       emax = ffabs(e) > emax ? ffabs(e) : emax;
     }
   if (!(emax <= T(0.05))) return false;
   T Y[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) Y[i] = T(0.5) * E[i];
-#pragma unroll
+  // at most six iterations; an iteration that returns Y unchanged is a fixed point (every later one
+  // would return the same Y), so stopping there gives the six-iteration result bit for bit
+#pragma unroll 1
   for (int it = 0; it < 6; ++it) {
     T Yn[9];
+    bool same = true;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
-      for (int b = 0; b < 3; ++b)
-        Yn[a * 3 + b] = T(0.5) * (E[a * 3 + b] - (Y[a * 3 + 0] * Y[0 * 3 + b] + Y[a * 3 + 1] * Y[1 * 3 + b] +
-                                                  Y[a * 3 + 2] * Y[2 * 3 + b]));
+      for (int b = a; b < 3; ++b) {
+        const T y = T(0.5) * (E[a * 3 + b] - (Y[a * 3 + 0] * Y[0 * 3 + b] + Y[a * 3 + 1] * Y[1 * 3 + b] +
+                                              Y[a * 3 + 2] * Y[2 * 3 + b]));
+        Yn[a * 3 + b] = Yn[b * 3 + a] = y;
+        same = same && y == Y[a * 3 + b];
+      }
 #pragma unroll
     for (int i = 0; i < 9; ++i) Y[i] = Yn[i];
+    if (same) break;
   }
   T M[9], Mc[9];
 #pragma unroll
