@@ -285,58 +285,60 @@ __global__ void __launch_bounds__(1024) k_plan(Geom<DIM> g, uint32_t* __restrict
     }
     __syncthreads();
   }
+  // touched if any block b - o, o in {0,1}^DIM, holds particles; with `sym` (plans kept over
+  // several substeps) any block b + o, o in {-1,0,1}^DIM
+  const auto touched_block = [&](int b) -> uint32_t {
+    if (use_bits) return (tch_bits[b >> 5] >> (b & 31)) & 1u;
+    int bc[DIM];
+    block_coords<DIM>(g, b, bc);
+    if (!sym) {
+      uint32_t tch = 0;
+#pragma unroll
+      for (int o = 0; o < (1 << DIM); ++o) {
+        int nb_id = 0;
+        bool ok = true;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const int cc = bc[d] - ((o >> (DIM - 1 - d)) & 1);
+          ok = ok && cc >= 0;
+          nb_id = nb_id * g.nb + cc;
+        }
+        if (ok && block_count[nb_id] > 0) tch = 1;
+      }
+      return tch;
+    }
+    constexpr int NO = DIM == 3 ? 27 : 9;
+    for (int o = 0; o < NO; ++o) {
+      int nb_id = 0, r = o;
+      bool ok = true;
+#pragma unroll
+      for (int d = DIM - 1; d >= 0; --d) {
+        const int cc = bc[d] + (r % 3) - 1;
+        r /= 3;
+        ok = ok && cc >= 0 && cc < g.nb;
+      }
+      if (!ok) continue;
+      r = o;
+      int mul = 1;
+#pragma unroll
+      for (int d = DIM - 1; d >= 0; --d) {
+        nb_id += (bc[d] + (r % 3) - 1) * mul;
+        mul *= g.nb;
+        r /= 3;
+      }
+      if (block_count[nb_id] > 0) return 1u;
+    }
+    return 0u;
+  };
+  // one block per thread and pass (coalesced reads and writes); the next pass's count is loaded
+  // before this pass's scan so that its latency overlaps the scan
   Scan4 carry{0, 0, 0, 0};  // (particles, chunks, touched, occupied)
+  uint32_t c = (int)threadIdx.x < g.nblocks ? block_count[threadIdx.x] : 0u;
   for (int seg = 0; seg < g.nblocks; seg += blockDim.x) {
     const int b = seg + threadIdx.x;
-    uint32_t c = 0, tch = 0;
-    if (b < g.nblocks) {
-      c = block_count[b];
-      int bc[DIM];
-      block_coords<DIM>(g, b, bc);
-      // touched if any block b - o, o in {0,1}^DIM, holds particles; with `sym` (plans kept over
-      // several substeps) any block b + o, o in {-1,0,1}^DIM
-      if (use_bits) {
-        tch = (tch_bits[b >> 5] >> (b & 31)) & 1u;
-      } else if (!sym) {
-#pragma unroll
-        for (int o = 0; o < (1 << DIM); ++o) {
-          int nb_id = 0;
-          bool ok = true;
-#pragma unroll
-          for (int d = 0; d < DIM; ++d) {
-            const int cc = bc[d] - ((o >> (DIM - 1 - d)) & 1);
-            ok = ok && cc >= 0;
-            nb_id = nb_id * g.nb + cc;
-          }
-          if (ok && block_count[nb_id] > 0) tch = 1;
-        }
-      } else {
-        constexpr int NO = DIM == 3 ? 27 : 9;
-        for (int o = 0; o < NO; ++o) {
-          int nb_id = 0, r = o;
-          bool ok = true;
-#pragma unroll
-          for (int d = DIM - 1; d >= 0; --d) {
-            const int cc = bc[d] + (r % 3) - 1;
-            r /= 3;
-            ok = ok && cc >= 0 && cc < g.nb;
-          }
-          if (!ok) continue;
-          r = o;
-          int mul = 1;
-#pragma unroll
-          for (int d = DIM - 1; d >= 0; --d) {
-            nb_id += (bc[d] + (r % 3) - 1) * mul;
-            mul *= g.nb;
-            r /= 3;
-          }
-          if (block_count[nb_id] > 0) {
-            tch = 1;
-            break;
-          }
-        }
-      }
-    }
+    const int bn = b + blockDim.x;
+    const uint32_t c_next = bn < g.nblocks ? block_count[bn] : 0u;
+    const uint32_t tch = b < g.nblocks ? touched_block(b) : 0u;
     const uint32_t nch = (c + kChunk - 1) / kChunk;
     Scan4 v{c, nch, tch, c > 0 ? 1u : 0u}, tot;
     Scan4 ex = block_exclusive_scan4(v, &tot, warp_buf);
@@ -353,6 +355,7 @@ __global__ void __launch_bounds__(1024) k_plan(Geom<DIM> g, uint32_t* __restrict
       if (c > 0) occupied[carry.d + ex.d] = make_int4(b, (int)start, (int)c, 0);
     }
     carry.a += tot.a; carry.b += tot.b; carry.c += tot.c; carry.d += tot.d;
+    c = c_next;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1155,31 +1158,23 @@ __global__ void __launch_bounds__(kThreads) k_p2g_det(KParams<T> kp, Geom<DIM> g
       const int cz = min(kChunk, occ.z - c0);
       const uint32_t s0 = (uint32_t)(occ.y + c0);
       __syncthreads();  // tiles zeroed / previous chunk's records consumed
-      for (int l = threadIdx.x; l < cz; l += 2 * blockDim.x) {
-        const int l2 = l + blockDim.x;
-        const bool two = l2 < cz;
-        const uint32_t p1 = perm[s0 + l], p2 = perm[s0 + (two ? l2 : l)];
-        P2GIn<DIM, T> in[2];
-        p2g_load<DIM, T>(kp, P, p1, in[0]);
-        p2g_load<DIM, T>(kp, P, p2, in[1]);
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          if (u == 1 && !two) break;
-          const int lu = u ? l2 : l;
-          T rec[RS];
-          int cell = -1;
-          int base[DIM];
-          if (p2g_record<DIM, T>(kp, g, in[u], org, rec, cell, status, fallbacks, base) != kRecTile) {
-            if (cell < 0) raise_status(status, FFMPM_STATUS_OOB);  // a fresh plan has no strays
-            cell = -1;
-          }
-#pragma unroll
-          for (int i = RF; i < RS; ++i) rec[i] = T(0);
-          Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)lu * RS);
-#pragma unroll
-          for (int i = 0; i < RS / 4; ++i) dst[i] = Node4<T>{rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]};
-          cells[lu] = cell;
+      // one particle per thread at a time (two in flight cost more registers than they gain)
+      for (int l = threadIdx.x; l < cz; l += blockDim.x) {
+        P2GIn<DIM, T> in;
+        p2g_load<DIM, T>(kp, P, perm[s0 + l], in);
+        T rec[RS];
+        int cell = -1;
+        int base[DIM];
+        if (p2g_record<DIM, T>(kp, g, in, org, rec, cell, status, fallbacks, base) != kRecTile) {
+          if (cell < 0) raise_status(status, FFMPM_STATUS_OOB);  // a fresh plan has no strays
+          cell = -1;
         }
+#pragma unroll
+        for (int i = RF; i < RS; ++i) rec[i] = T(0);
+        Node4<T>* dst = reinterpret_cast<Node4<T>*>(recs + (size_t)l * RS);
+#pragma unroll
+        for (int i = 0; i < RS / 4; ++i) dst[i] = Node4<T>{rec[4 * i], rec[4 * i + 1], rec[4 * i + 2], rec[4 * i + 3]};
+        cells[l] = cell;
       }
       __syncthreads();
       {
