@@ -65,3 +65,58 @@ def test_snow_3d_substeps_match_oracle(dtype):
     # the clamp acted: every singular value of F is inside the band after a snow G2P
     sv = np.linalg.svd(n(gF), compute_uv=False)
     assert sv.min() > 0.975 - 1e-4 and sv.max() < 1.0075 + 1e-4
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_snow_3d_resident_solver_matches_oracle(dtype):
+    """The snow model through the resident solver (fused G2P + next-substep P2G: the hardening of
+    the P2G half uses the Jp its own G2P half just updated) against the oracle's substeps."""
+    from femflow_gb300.solver import MPMSolver
+
+    s = scene(seed=9)
+    res, dt, g, h, steps = s["res"], 1e-4, -9.8, 10.0, 6
+    solver = MPMSolver(torch.tensor(s["x"]), res=res, dt=dt, gravity=g, volume=s["vol"], hardening=h,
+                       mass=torch.tensor(s["mass"]), mu_0=torch.tensor(s["mu"]), lambda_0=torch.tensor(s["lam"]),
+                       v=torch.tensor(s["v"]), F=torch.tensor(s["F"]), C=torch.tensor(s["C"]),
+                       Jp=torch.tensor(s["Jp"]), dtype=dtype, model="snow")
+    solver.step(steps, check=True)
+    got = solver.state()
+    ox, ov, oF, oC, oJ = (s[k].copy() for k in ("x", "v", "F", "C", "Jp"))
+    for _ in range(steps):
+        O.substep_3d(res, float(res), h, 1 / res, dt, s["vol"], g, ox, s["mass"], s["mu"], s["lam"], ov, oF, oC,
+                     oJ, "snow")
+    tol = TOL[dtype]
+    close(n(got["x"]), ox, 5 * tol["x"], scale=1.0, what="x")
+    close(n(got["v"]), ov, 5 * tol["v"], scale=np.abs(ov).max(), what="v")
+    close(n(got["F"]), oF, 20 * tol["F"], scale=1.0, what="F")
+    close(n(got["Jp"]).reshape(-1, 1), oJ, 20 * tol["F"], scale=1.0, what="Jp")
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_snow_2d_resident_solver_matches_oracle(dtype):
+    """2D snow through the resident solver against the oracle's 2D substeps (x, v, Jp; 2D F is
+    defined up to the sign of LAPACK's SVD, see two_d/g2p.py:37-43)."""
+    from femflow_gb300.solver import MPMSolver
+
+    rng = np.random.default_rng(4)
+    N, res, dt, g, h, steps = 1200, 32, 1e-4, -9.8, 10.0, 6
+    x = rng.uniform(0.3, 0.7, (N, 2))
+    vol = 0.16 / N
+    E, nu = 2e3, 0.25
+    mu, lam = E / (2 * (1 + nu)), E * nu / ((1 + nu) * (1 - 2 * nu))
+    v = rng.normal(0, 0.2, (N, 2))
+    F = np.array([np.diag(rng.uniform(0.95, 1.03, 2)) for _ in range(N)])
+    C = rng.normal(0, 0.5, (N, 2, 2))
+    Jp = rng.uniform(0.9, 1.1, (N, 1))
+    solver = MPMSolver(torch.tensor(x), res=res, dt=dt, gravity=g, volume=vol, hardening=h, mass=vol, mu_0=mu,
+                       lambda_0=lam, v=torch.tensor(v), F=torch.tensor(F), C=torch.tensor(C), Jp=torch.tensor(Jp),
+                       dtype=dtype, model="snow")
+    solver.step(steps, check=True)
+    got = solver.state()
+    ox, ov, oF, oC, oJ = x.copy(), v.copy(), F.copy(), C.copy(), Jp.copy()
+    for _ in range(steps):
+        O.substep_2d(res, float(res), h, mu, lam, vol, 1 / res, dt, vol, g, ox, ov, oF, oC, oJ, "snow")
+    tol = TOL[dtype]
+    close(n(got["x"]), ox, 5 * tol["x"], scale=1.0, what="x")
+    close(n(got["v"]), ov, 5 * tol["v"], scale=np.abs(ov).max(), what="v")
+    close(n(got["Jp"]).reshape(-1, 1), oJ, 20 * tol["F"], scale=1.0, what="Jp")
