@@ -349,7 +349,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--fp64-steps", type=int, default=200, help="substeps of the float32-vs-float64 error run")
+    ap.add_argument("--fp64-steps", type=int, default=1000, help="substeps of the float32-vs-float64 error run")
     ap.add_argument("--cpu-steps", type=int, default=8, help="substeps of the serial CPU-port baseline (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -101,6 +101,9 @@ bool make_layout(const ffmpm_params& p, int64_t n, Layout* L) {
   L->off_gridA = take(node_bytes * L->nnodes);
   L->off_gridB = take(node_bytes * L->nnodes);
   L->off_stage = take(p.deterministic ? node_bytes * tile_nodes * L->nblocks : 0);
+  // the plan kernels' per-block prefixes (3 x nblocks) and per-CTA totals and offsets
+  L->off_plan_pref = take(sizeof(uint32_t) * 3 * L->nblocks);
+  L->off_plan_cta = take(2 * 16 * ((L->nblocks + kPlanCta - 1) / kPlanCta));
   L->total = off;
   return true;
 }
@@ -168,6 +171,8 @@ struct Ws {
   uint32_t *block_count, *block_start, *block_cnt, *touched, *tmark, *keys_next, *keys0, *keys1, *vals0, *vals1, *hist;
   int4 *chunks, *occupied;
   void *gridA, *gridB, *stage;
+  uint32_t* plan_pref;
+  Scan4 *cta_tot, *cta_off;
 };
 
 Ws bind(void* ws, const Layout& L) {
@@ -190,6 +195,9 @@ Ws bind(void* ws, const Layout& L) {
   w.gridA = w.base + L.off_gridA;
   w.gridB = w.base + L.off_gridB;
   w.stage = w.base + L.off_stage;
+  w.plan_pref = reinterpret_cast<uint32_t*>(w.base + L.off_plan_pref);
+  w.cta_tot = reinterpret_cast<Scan4*>(w.base + L.off_plan_cta);
+  w.cta_off = w.cta_tot + (L.nblocks + kPlanCta - 1) / kPlanCta;
   return w;
 }
 
@@ -287,9 +295,13 @@ void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const PV
              &ks, perm, flag);
   if (tm) tm->end(1 + L.passes);
   if (tm) tm->begin(2);
-  k_plan<DIM><<<1, 1024, 0, s>>>(g, w.block_count, w.block_start, w.block_cnt, w.chunks, w.touched, w.tmark,
-                                 w.occupied, w.hdr, flag, sym >= 0 ? sym : (flag ? 1 : 0));
-  if (tm) tm->end(1);
+  const int ncta = (int)((L.nblocks + kPlanCta - 1) / kPlanCta);
+  k_plan_local<DIM><<<ncta, kPlanCta, 0, s>>>(g, w.block_count, w.block_start, w.block_cnt, w.tmark, w.plan_pref,
+                                              w.cta_tot, flag, sym >= 0 ? sym : (flag ? 1 : 0));
+  k_plan_offsets<<<1, kPlanCta, 0, s>>>(w.cta_tot, w.cta_off, ncta, w.hdr, flag);
+  k_plan_write<DIM><<<ncta, kPlanCta, 0, s>>>(g, w.block_count, w.block_start, w.block_cnt, w.tmark, w.plan_pref,
+                                              w.cta_off, w.chunks, w.touched, w.occupied, flag);
+  if (tm) tm->end(3);
 }
 
 template <int DIM, typename T>
@@ -713,9 +725,9 @@ int ffmpm_plan_info(const ffmpm_params* p, int64_t n, int64_t* info) {
   info[2] = L.nblocks;
   info[3] = L.key_bits;
   info[4] = L.passes;
-  // digit histogram + one kernel per radix pass + plan + P2G + grid + G2P (+ the re-sort decision
-  // of cadenced runs)
-  info[5] = L.passes + 5 + (sort_every(*p) > 1 ? 1 : 0);
+  // digit histogram + one kernel per radix pass + 3 plan kernels + P2G + grid + G2P (+ the re-sort
+  // decision of cadenced runs)
+  info[5] = L.passes + 7 + (sort_every(*p) > 1 ? 1 : 0);
   info[6] = L.tile;
   info[7] = L.max_chunks;
   return FFMPM_OK;
@@ -766,7 +778,7 @@ int ffmpm_check_collision_points(const ffmpm_params* p, const double* points, co
 int ffmpm_kernels_per_call(const ffmpm_params* p, int64_t n, int32_t nsteps, int64_t* count) {
   Layout L;
   if (!p || !count || nsteps < 0 || !make_layout(*p, n, &L)) return FFMPM_ERR_BADARG;
-  const int64_t sort = 1 + L.passes + 1;  // digit histogram, one kernel per pass, plan
+  const int64_t sort = 1 + L.passes + 3;  // digit histogram, one kernel per pass, three plan kernels
   if (n == 0 || nsteps == 0) {
     *count = 0;
   } else if (fused(*p, nsteps)) {

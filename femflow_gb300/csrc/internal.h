@@ -34,7 +34,7 @@ struct Layout {
   int64_t n = 0, nblocks = 0, nnodes = 0, max_chunks = 0, ntiles = 0;
   size_t off_block_count = 0, off_block_start = 0, off_block_cnt = 0, off_chunks = 0, off_touched = 0, off_tmark = 0,
          off_occupied = 0, off_keys_next = 0, off_keys0 = 0, off_keys1 = 0, off_vals0 = 0, off_vals1 = 0,
-         off_hist = 0, off_gridA = 0, off_gridB = 0, off_stage = 0, total = 0;
+         off_hist = 0, off_gridA = 0, off_gridB = 0, off_stage = 0, off_plan_pref = 0, off_plan_cta = 0, total = 0;
 };
 
 bool make_layout(const ffmpm_params& p, int64_t n, Layout* L);

@@ -185,186 +185,200 @@ __global__ void __launch_bounds__(kThreads) k_keys(KParams<T> kp, Geom<DIM> g, P
 }
 
 // ----------------------------------------------------------------------------------------------
-// k_plan: one CTA of 1024 threads over all blocks.  Produces block starts (exclusive scan of the
-// histogram), chunks of at most kChunk particles, the list of occupied blocks, and the touched
-// blocks (occupied blocks dilated by +1 along every axis, because a stencil based in block b
-// reaches 2 nodes into block b+1).  Re-zeroes the histogram for the next substep.
+// The plan: block starts (exclusive scan of the histogram), chunks of at most kChunk particles, the
+// list of occupied blocks, and the touched blocks (occupied blocks dilated by +1 along every axis,
+// because a stencil based in block b reaches 2 nodes into block b+1; by +-1 when the plan is kept
+// over several substeps).  Three launches over CTAs of 1024 blocks (k_plan_local: values and local
+// prefixes; k_plan_offsets: prefixes of the CTA totals; k_plan_write: final offsets and lists), so
+// that no CTA waits on another.  The last one re-zeroes the histogram for the next substep.
 struct Scan4 {
   uint32_t a, b, c, d;
 };
 
-constexpr int kPlanBitmapWords = 5632;  // 22 KB of shared memory per bitmap: grids of up to 180,224 blocks
-
-__device__ __forceinline__ Scan4 block_exclusive_scan4(Scan4 v, Scan4* total, Scan4* warp_buf) {
+// Exclusive scan of KB Scan4 values per thread over the CTA, part j of every thread before part
+// j + 1 (the thread's parts cover blocks j * blockDim + threadIdx): ex[j] is the prefix of part j
+// of this thread, *total the sum of everything.  One set of barriers for all KB parts.
+template <int KB>
+__device__ __forceinline__ void block_exclusive_scan4_parts(const Scan4 (&v)[KB], Scan4 (&ex)[KB], Scan4* total,
+                                                            Scan4 (*warp_buf)[32]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  Scan4 inc = v;
+  Scan4 inc[KB];
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t ta = __shfl_up_sync(0xffffffffu, inc.a, o), tb = __shfl_up_sync(0xffffffffu, inc.b, o);
-    const uint32_t tc = __shfl_up_sync(0xffffffffu, inc.c, o), td = __shfl_up_sync(0xffffffffu, inc.d, o);
-    if (lane >= o) {
-      inc.a += ta; inc.b += tb; inc.c += tc; inc.d += td;
-    }
-  }
-  if (lane == 31) warp_buf[warp] = inc;
-  __syncthreads();
-  if (warp == 0) {
-    Scan4 w = lane < nwarps ? warp_buf[lane] : Scan4{0, 0, 0, 0};
+  for (int j = 0; j < KB; ++j) {
+    inc[j] = v[j];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t ta = __shfl_up_sync(0xffffffffu, w.a, o), tb = __shfl_up_sync(0xffffffffu, w.b, o);
-      const uint32_t tc = __shfl_up_sync(0xffffffffu, w.c, o), td = __shfl_up_sync(0xffffffffu, w.d, o);
+      const uint32_t ta = __shfl_up_sync(0xffffffffu, inc[j].a, o), tb = __shfl_up_sync(0xffffffffu, inc[j].b, o);
+      const uint32_t tc = __shfl_up_sync(0xffffffffu, inc[j].c, o), td = __shfl_up_sync(0xffffffffu, inc[j].d, o);
       if (lane >= o) {
-        w.a += ta; w.b += tb; w.c += tc; w.d += td;
+        inc[j].a += ta; inc[j].b += tb; inc[j].c += tc; inc[j].d += td;
       }
     }
-    if (lane < nwarps) warp_buf[lane] = w;
+    if (lane == 31) warp_buf[j][warp] = inc[j];
   }
   __syncthreads();
-  Scan4 prev = warp > 0 ? warp_buf[warp - 1] : Scan4{0, 0, 0, 0};
-  Scan4 ex{prev.a + inc.a - v.a, prev.b + inc.b - v.b, prev.c + inc.c - v.c, prev.d + inc.d - v.d};
-  *total = warp_buf[nwarps - 1];
+  if (warp == 0) {
+    // scan the KB x nwarps warp totals in part-major order
+    Scan4 carry{0, 0, 0, 0};
+#pragma unroll
+    for (int j = 0; j < KB; ++j) {
+      Scan4 w = lane < nwarps ? warp_buf[j][lane] : Scan4{0, 0, 0, 0};
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t ta = __shfl_up_sync(0xffffffffu, w.a, o), tb = __shfl_up_sync(0xffffffffu, w.b, o);
+        const uint32_t tc = __shfl_up_sync(0xffffffffu, w.c, o), td = __shfl_up_sync(0xffffffffu, w.d, o);
+        if (lane >= o) {
+          w.a += ta; w.b += tb; w.c += tc; w.d += td;
+        }
+      }
+      w.a += carry.a; w.b += carry.b; w.c += carry.c; w.d += carry.d;
+      if (lane < nwarps) warp_buf[j][lane] = w;  // inclusive over parts < j and warps <= lane
+      carry.a = __shfl_sync(0xffffffffu, w.a, nwarps - 1);
+      carry.b = __shfl_sync(0xffffffffu, w.b, nwarps - 1);
+      carry.c = __shfl_sync(0xffffffffu, w.c, nwarps - 1);
+      carry.d = __shfl_sync(0xffffffffu, w.d, nwarps - 1);
+    }
+  }
   __syncthreads();
-  return ex;
+#pragma unroll
+  for (int j = 0; j < KB; ++j) {
+    Scan4 prev;
+    if (warp > 0) prev = warp_buf[j][warp - 1];
+    else if (j > 0) prev = warp_buf[j - 1][nwarps - 1];
+    else prev = Scan4{0, 0, 0, 0};
+    ex[j] = Scan4{prev.a + inc[j].a - v[j].a, prev.b + inc[j].b - v[j].b, prev.c + inc[j].c - v[j].c,
+                  prev.d + inc[j].d - v[j].d};
+  }
+  *total = warp_buf[KB - 1][nwarps - 1];
+  __syncthreads();
 }
 
+// Touched test of block b, gather form: any block b - o, o in {0,1}^DIM, holds particles; with `sym`
+// any block b + o, o in {-1,0,1}^DIM (the histogram is small and stays in L2).
 template <int DIM>
-__global__ void __launch_bounds__(1024) k_plan(Geom<DIM> g, uint32_t* __restrict__ block_count,
-                                               uint32_t* __restrict__ block_start, uint32_t* __restrict__ block_cnt,
-                                               int4* __restrict__ chunks, uint32_t* __restrict__ touched,
-                                               uint32_t* __restrict__ tmark, int4* __restrict__ occupied,
-                                               WsHeader* hdr, const uint32_t* __restrict__ sort_flag, int sym) {
-  if (sort_flag && *sort_flag == 0u) {
-    // no re-sort this substep: keep the plan, only clear the histogram G2P accumulates
-    for (int b = threadIdx.x; b < g.nblocks; b += blockDim.x) block_count[b] = 0;
-    return;
-  }
-  __shared__ Scan4 warp_buf[32];
-  // Touched blocks as a bitmap: every occupied block sets the bits of the blocks its stencils can
-  // reach (b + {0,1}^DIM, or b + {-1,0,1}^DIM with `sym`), so the work is proportional to the
-  // occupied blocks, not to all blocks times their neighbourhood.  Grids with more blocks than the
-  // bitmap holds test the neighbourhood of every block against the histogram instead.
-  __shared__ uint32_t occ_bits[kPlanBitmapWords];
-  __shared__ uint32_t tch_bits[kPlanBitmapWords];
-  const bool use_bits = g.nblocks <= kPlanBitmapWords * 32;
-  if (use_bits) {
-    const int nwords = (g.nblocks + 31) / 32;
-    for (int wd = threadIdx.x; wd < nwords; wd += blockDim.x) tch_bits[wd] = 0u;
-    for (int wd = threadIdx.x >> 5; wd < nwords; wd += blockDim.x >> 5) {
-      const int b = wd * 32 + (threadIdx.x & 31);
-      const unsigned m = __ballot_sync(0xffffffffu, b < g.nblocks && block_count[b] > 0);
-      if ((threadIdx.x & 31) == 0) occ_bits[wd] = m;
-    }
-    __syncthreads();
-    const int NO = sym ? (DIM == 3 ? 27 : 9) : (1 << DIM);
-    for (int b = threadIdx.x; b < g.nblocks; b += blockDim.x) {
-      if (!((occ_bits[b >> 5] >> (b & 31)) & 1u)) continue;
-      int bc[DIM];
-      block_coords<DIM>(g, b, bc);
-      for (int o = 0; o < NO; ++o) {
-        int id = 0, r = o;
-        bool ok = true;
+__device__ __forceinline__ uint32_t plan_touched(const Geom<DIM>& g, const uint32_t* __restrict__ block_count, int b,
+                                                 int sym) {
+  int bc[DIM];
+  block_coords<DIM>(g, b, bc);
+  if (!sym) {
 #pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          // offsets of axis d: sym -> (o / 3^(DIM-1-d)) % 3 - 1, else bit DIM-1-d of o
-          int od;
-          if (sym) {
-            int div = 1;
-#pragma unroll
-            for (int e = d + 1; e < DIM; ++e) div *= 3;
-            od = (r / div) % 3 - 1;
-          } else {
-            od = (o >> (DIM - 1 - d)) & 1;
-          }
-          const int cc = bc[d] + od;
-          ok = ok && cc >= 0 && cc < g.nb;
-          id = id * g.nb + cc;
-        }
-        if (ok) atomicOr(&tch_bits[id >> 5], 1u << (id & 31));
-      }
-    }
-    __syncthreads();
-  }
-  // touched if any block b - o, o in {0,1}^DIM, holds particles; with `sym` (plans kept over
-  // several substeps) any block b + o, o in {-1,0,1}^DIM
-  const auto touched_block = [&](int b) -> uint32_t {
-    if (use_bits) return (tch_bits[b >> 5] >> (b & 31)) & 1u;
-    int bc[DIM];
-    block_coords<DIM>(g, b, bc);
-    if (!sym) {
-      uint32_t tch = 0;
-#pragma unroll
-      for (int o = 0; o < (1 << DIM); ++o) {
-        int nb_id = 0;
-        bool ok = true;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          const int cc = bc[d] - ((o >> (DIM - 1 - d)) & 1);
-          ok = ok && cc >= 0;
-          nb_id = nb_id * g.nb + cc;
-        }
-        if (ok && block_count[nb_id] > 0) tch = 1;
-      }
-      return tch;
-    }
-    constexpr int NO = DIM == 3 ? 27 : 9;
-    for (int o = 0; o < NO; ++o) {
-      int nb_id = 0, r = o;
+    for (int o = 0; o < (1 << DIM); ++o) {
+      int nb_id = 0;
       bool ok = true;
 #pragma unroll
-      for (int d = DIM - 1; d >= 0; --d) {
-        const int cc = bc[d] + (r % 3) - 1;
-        r /= 3;
-        ok = ok && cc >= 0 && cc < g.nb;
+      for (int d = 0; d < DIM; ++d) {
+        const int cc = bc[d] - ((o >> (DIM - 1 - d)) & 1);
+        ok = ok && cc >= 0;
+        nb_id = nb_id * g.nb + cc;
       }
-      if (!ok) continue;
-      r = o;
-      int mul = 1;
-#pragma unroll
-      for (int d = DIM - 1; d >= 0; --d) {
-        nb_id += (bc[d] + (r % 3) - 1) * mul;
-        mul *= g.nb;
-        r /= 3;
-      }
-      if (block_count[nb_id] > 0) return 1u;
+      if (ok && block_count[nb_id] > 0) return 1u;
     }
     return 0u;
-  };
-  // one block per thread and pass (coalesced reads and writes); the next pass's count is loaded
-  // before this pass's scan so that its latency overlaps the scan
-  Scan4 carry{0, 0, 0, 0};  // (particles, chunks, touched, occupied)
-  uint32_t c = (int)threadIdx.x < g.nblocks ? block_count[threadIdx.x] : 0u;
-  for (int seg = 0; seg < g.nblocks; seg += blockDim.x) {
-    const int b = seg + threadIdx.x;
-    const int bn = b + blockDim.x;
-    const uint32_t c_next = bn < g.nblocks ? block_count[bn] : 0u;
-    const uint32_t tch = b < g.nblocks ? touched_block(b) : 0u;
-    const uint32_t nch = (c + kChunk - 1) / kChunk;
-    Scan4 v{c, nch, tch, c > 0 ? 1u : 0u}, tot;
-    Scan4 ex = block_exclusive_scan4(v, &tot, warp_buf);
-    if (b < g.nblocks) {
-      const uint32_t start = carry.a + ex.a;
-      block_start[b] = start;
-      block_cnt[b] = c;
-      for (uint32_t q = 0; q < nch; ++q) {
-        const uint32_t s = start + q * kChunk;
-        chunks[carry.b + ex.b + q] = make_int4(b, (int)s, (int)min((uint32_t)kChunk, c - q * kChunk), 0);
-      }
-      if (tch) touched[carry.c + ex.c] = (uint32_t)b;
-      tmark[b] = tch;
-      if (c > 0) occupied[carry.d + ex.d] = make_int4(b, (int)start, (int)c, 0);
-    }
-    carry.a += tot.a; carry.b += tot.b; carry.c += tot.c; carry.d += tot.d;
-    c = c_next;
   }
-  __syncthreads();
+  constexpr int NO = DIM == 3 ? 27 : 9;
+#pragma unroll
+  for (int o = 0; o < NO; ++o) {
+    int nb_id = 0, r = o;
+    bool ok = true;
+#pragma unroll
+    for (int d = DIM - 1; d >= 0; --d) {
+      const int cc = bc[d] + (r % 3) - 1;
+      r /= 3;
+      ok = ok && cc >= 0 && cc < g.nb;
+    }
+    if (!ok) continue;
+    r = o;
+    int mul = 1;
+#pragma unroll
+    for (int d = DIM - 1; d >= 0; --d) {
+      nb_id += (bc[d] + (r % 3) - 1) * mul;
+      mul *= g.nb;
+      r /= 3;
+    }
+    if (block_count[nb_id] > 0) return 1u;
+  }
+  return 0u;
+}
+
+constexpr int kPlanCta = 1024;  // blocks per CTA of the plan kernels
+
+// Per block: count, touched mark, and the prefixes of (particles, chunks, touched, occupied) within
+// its CTA's 1024 blocks (particles in block_start, the others in pref[0..2][nblocks]); per CTA: the
+// totals.  Nothing is done on a substep that keeps its plan (sort_flag 0).
+template <int DIM>
+__global__ void __launch_bounds__(kPlanCta) k_plan_local(Geom<DIM> g, const uint32_t* __restrict__ block_count,
+                                                         uint32_t* __restrict__ block_start,
+                                                         uint32_t* __restrict__ block_cnt, uint32_t* __restrict__ tmark,
+                                                         uint32_t* __restrict__ pref, Scan4* __restrict__ cta_tot,
+                                                         const uint32_t* __restrict__ sort_flag, int sym) {
+  if (sort_flag && *sort_flag == 0u) return;
+  __shared__ Scan4 part_buf[1][32];
+  const int b = blockIdx.x * kPlanCta + threadIdx.x;
+  uint32_t c = 0, tch = 0;
+  if (b < g.nblocks) {
+    c = block_count[b];
+    tch = plan_touched<DIM>(g, block_count, b, sym);
+  }
+  const Scan4 v[1] = {Scan4{c, (c + kChunk - 1) / kChunk, tch, c > 0 ? 1u : 0u}};
+  Scan4 ex[1], tot;
+  block_exclusive_scan4_parts<1>(v, ex, &tot, part_buf);
+  if (b < g.nblocks) {
+    block_start[b] = ex[0].a;
+    pref[b] = ex[0].b;
+    pref[g.nblocks + b] = ex[0].c;
+    pref[2 * g.nblocks + b] = ex[0].d;
+    block_cnt[b] = c;
+    tmark[b] = tch;
+  }
+  if (threadIdx.x == 0) cta_tot[blockIdx.x] = tot;
+}
+
+// One CTA: exclusive prefixes of the CTA totals, and the plan's totals into the header.
+static __global__ void __launch_bounds__(kPlanCta) k_plan_offsets(const Scan4* __restrict__ cta_tot, Scan4* __restrict__ cta_off,
+                                                           int ncta, WsHeader* hdr, const uint32_t* __restrict__ sort_flag) {
+  if (sort_flag && *sort_flag == 0u) return;
+  __shared__ Scan4 part_buf[1][32];
+  Scan4 carry{0, 0, 0, 0};
+  for (int base = 0; base < ncta; base += kPlanCta) {
+    const int i = base + threadIdx.x;
+    const Scan4 v[1] = {i < ncta ? cta_tot[i] : Scan4{0, 0, 0, 0}};
+    Scan4 ex[1], tot;
+    block_exclusive_scan4_parts<1>(v, ex, &tot, part_buf);
+    if (i < ncta) cta_off[i] = Scan4{carry.a + ex[0].a, carry.b + ex[0].b, carry.c + ex[0].c, carry.d + ex[0].d};
+    carry.a += tot.a; carry.b += tot.b; carry.c += tot.c; carry.d += tot.d;
+  }
   if (threadIdx.x == 0) {
     hdr->n_valid = carry.a;
     hdr->n_chunks = carry.b;
     hdr->n_touched = carry.c;
     hdr->n_occupied = carry.d;
   }
-  for (int b = threadIdx.x; b < g.nblocks; b += blockDim.x) block_count[b] = 0;
+}
+
+// Final block starts, the chunks, the touched and occupied lists; re-zeroes the histogram (also on
+// substeps that keep their plan, where nothing else is written).
+template <int DIM>
+__global__ void __launch_bounds__(kPlanCta) k_plan_write(Geom<DIM> g, uint32_t* __restrict__ block_count,
+                                                         uint32_t* __restrict__ block_start,
+                                                         const uint32_t* __restrict__ block_cnt,
+                                                         const uint32_t* __restrict__ tmark,
+                                                         const uint32_t* __restrict__ pref,
+                                                         const Scan4* __restrict__ cta_off, int4* __restrict__ chunks,
+                                                         uint32_t* __restrict__ touched, int4* __restrict__ occupied,
+                                                         const uint32_t* __restrict__ sort_flag) {
+  const int b = blockIdx.x * kPlanCta + threadIdx.x;
+  if (b >= g.nblocks) return;
+  if (!(sort_flag && *sort_flag == 0u)) {
+    const Scan4 off = cta_off[blockIdx.x];
+    const uint32_t c = block_cnt[b], start = off.a + block_start[b];
+    block_start[b] = start;
+    const uint32_t nch = (c + kChunk - 1) / kChunk, ch0 = off.b + pref[b];
+    for (uint32_t q = 0; q < nch; ++q)
+      chunks[ch0 + q] = make_int4(b, (int)(start + q * kChunk), (int)min((uint32_t)kChunk, c - q * kChunk), 0);
+    if (tmark[b]) touched[off.c + pref[g.nblocks + b]] = (uint32_t)b;
+    if (c > 0) occupied[off.d + pref[2 * g.nblocks + b]] = make_int4(b, (int)start, (int)c, 0);
+  }
+  block_count[b] = 0;
 }
 
 // ----------------------------------------------------------------------------------------------

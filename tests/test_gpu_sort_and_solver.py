@@ -237,3 +237,20 @@ def test_fp64_diagnostics_match_numpy():
     J = np.linalg.det(F)
     el = (s["vol"] * (mu * ((F - R) ** 2).sum((1, 2)) + 0.5 * lam * (J - 1) ** 2)).sum()
     assert np.isclose(d["elastic"], el, rtol=1e-8)
+
+
+def test_float32_positions_within_1e_4_of_float64_after_1000_substeps():
+    """The accuracy target of the float32 path: the two-cube scene (2 x 32,768 particles, 64^3,
+    dt 5e-5, elastic CFL 0.25) run 1000 substeps in float32 and float64 through the resident
+    solver; the largest position difference stays below 1e-4 of the domain."""
+    from femflow_gb300.scenes import two_cubes
+
+    s = two_cubes(32768)
+    kw = dict(res=64, dt=5e-5, gravity=-9.8, volume=s["vol"], mass=s["mass"], mu_0=s["mu"], lambda_0=s["lam"],
+              v=torch.tensor(s["v"]))
+    a32 = MPMSolver(torch.tensor(s["x"]), dtype=torch.float32, **kw)
+    a64 = MPMSolver(torch.tensor(s["x"]), dtype=torch.float64, **kw)
+    a32.step(1000, check=True)
+    a64.step(1000, check=True)
+    err = (a32.positions().double() - a64.positions()).abs().max().item()
+    assert err < 1e-4, err

@@ -67,7 +67,7 @@ def test_kernels_per_call():
 
     info = (ctypes.c_int64 * 8)()
     N.call("ffmpm_plan_info", ctypes.byref(E.make_params(3, 128, torch.float32, 1 / 128, 128.0, 1e-4)), 1 << 20, info)
-    sort = 1 + info[4] + 1  # digit histogram, radix passes, plan
+    sort = 1 + info[4] + 3  # digit histogram, radix passes, three plan kernels
     every8 = 8 << 8
     # fused: (keys, sort, P2G) + (n - 1) (grid, fused) + the re-sorts at k = 8 + (grid, G2P)
     assert count(10, variant=every8) == (2 + sort) + 9 * 2 + 1 * sort + 2
