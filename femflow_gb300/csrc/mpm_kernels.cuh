@@ -3,13 +3,15 @@
 // Pipeline of one substep (all on one stream):
 //   k_keys         block key of every particle (three_d/p2g.py:50 base rule) + block histogram
 //   radix sort     stable, bit-exact permutation by key (sort.cu)
-//   k_plan         block offsets, work chunks, touched-block list (one CTA)
-//   k_p2g          stress + 3^d-node scatter into a shared-memory tile per block, one vector
-//                  atomic per touched node on flush          (three_d/p2g.py:14-80)
-//   k_grid_update  momentum -> velocity, gravity, clamp, walls over touched blocks only
-//                                                            (three_d/grid_op.py:5-47)
+//   k_plan_*       block offsets, work chunks, touched-block list (three launches)
+//   k_p2g_cells    stress + 3^d-node scatter by cell runs into a shared-memory tile per block, one
+//                  vector atomic per touched node on flush   (three_d/p2g.py:14-80)
+//   k_grid_update  momentum -> velocity, gravity, clamp, walls, planar colliders over touched
+//                  blocks only                               (three_d/grid_op.py:5-67)
 //   k_g2p          TMA-staged tile of grid velocities, gather v and APIC C, advect, update F
 //                                                            (three_d/g2p.py:9-59)
+//   k_g2p2g        G2P of one substep fused with P2G of the next (resident solver)
+// Sorting and planning run on the substeps that re-sort; the others keep the plan.
 #pragma once
 
 #include <algorithm>
