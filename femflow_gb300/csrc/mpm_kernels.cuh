@@ -1446,7 +1446,8 @@ __global__ void __launch_bounds__(kThreads) k_grid_update(KParams<T> kp, Geom<DI
       T vel[3] = {a.x, a.y, a.z};
       grid_node<DIM, T>(kp, I, vel, a.w);
       B[node] = Node4<T>{vel[0], vel[1], vel[2], a.w};
-      A[node] = Node4<T>{T(0), T(0), T(0), T(0)};
+      // re-zero A for the next P2G (a node that received nothing is zero already)
+      if (a.x != T(0) || a.y != T(0) || a.z != T(0) || a.w != T(0)) A[node] = Node4<T>{T(0), T(0), T(0), T(0)};
     }
   }
 }
