@@ -31,6 +31,7 @@ constexpr uint32_t kFlagAggregate = 1u << 30;
 constexpr uint32_t kFlagInclusive = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
 constexpr uint32_t kLookbackSpins = 1u << 22;
+constexpr int kLookbackBatch = 8;  // predecessor words read per look-back step
 
 // Digit histograms of all passes (ghist[pass][256]), one read of the keys.  Nearly sorted keys put
 // equal digits in neighbouring lanes, so each warp first merges equal digits (__match_any_sync).
@@ -160,24 +161,37 @@ __global__ void __launch_bounds__(kRsThreads) k_radix_onesweep(const uint32_t* _
       st_volatile(mine, kFlagInclusive | run);
     } else {
       st_volatile(mine, kFlagAggregate | run);
+      // walk back over the predecessors kLookbackBatch words at a time (the loads of a batch are
+      // in flight together): add published aggregates in order, stop at the first inclusive
+      // prefix, and re-read from the first word that is not published yet
       int t = (int)tile - 1;
       uint32_t spins = 0;
       while (t >= 0) {
-        const uint32_t w = ld_volatile(lookback + (size_t)t * 256 + d);
-        if (w & kFlagInclusive) {
-          excl += w & kValueMask;
-          break;
+        uint32_t w[kLookbackBatch];
+#pragma unroll
+        for (int j = 0; j < kLookbackBatch; ++j) w[j] = t - j >= 0 ? ld_volatile(lookback + (size_t)(t - j) * 256 + d) : 0u;
+        int used = 0;
+        bool found = false;
+#pragma unroll
+        for (int j = 0; j < kLookbackBatch; ++j) {
+          if (found || used < j || t - j < 0) continue;
+          if (w[j] & kFlagInclusive) {
+            excl += w[j] & kValueMask;
+            found = true;
+          } else if (w[j] & kFlagAggregate) {
+            excl += w[j] & kValueMask;
+            ++used;
+          }
         }
-        if (w & kFlagAggregate) {
-          excl += w & kValueMask;
-          --t;
-          continue;
+        if (found) break;
+        t -= used;
+        if (used == 0) {
+          if (++spins > kLookbackSpins) {
+            s_timeout = 1;
+            break;
+          }
+          __nanosleep(32);
         }
-        if (++spins > kLookbackSpins) {
-          s_timeout = 1;
-          break;
-        }
-        __nanosleep(32);
       }
       st_volatile(mine, kFlagInclusive | (excl + run));
     }
