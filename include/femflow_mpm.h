@@ -69,7 +69,11 @@ typedef struct ffmpm_params {
   int32_t wall_mode;    /* FFMPM_WALLS_* */
   int32_t deterministic;/* 1: P2G sums in a fixed order (bit-identical across runs) */
   int32_t block_size;   /* nodes per block side for work assignment; 0 = default */
-  int32_t variant;      /* kernel variant flags chosen by the autotuner; 0 = default */
+  int32_t variant;      /* kernel variant flags; 0 = default.  Bit 0: P2G scatters straight to the
+                         * grid; bit 1: P2G with one shared-memory atomic per (particle, node) (both
+                         * with a re-sort every substep); bit 2: ffmpm_substeps_sorted launches G2P
+                         * and P2G separately instead of the fused kernel; bits 8..15: substeps
+                         * between re-sorts of ffmpm_substeps_sorted (0 or 1: every substep) */
   double dx, inv_dx, dt;
   double gravity;       /* added to the axis-1 (y) grid velocity, as the reference */
   double volume;        /* particle volume (reference argument `volume`) */
