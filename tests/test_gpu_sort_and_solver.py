@@ -254,3 +254,30 @@ def test_float32_positions_within_1e_4_of_float64_after_1000_substeps():
     a64.step(1000, check=True)
     err = (a32.positions().double() - a64.positions()).abs().max().item()
     assert err < 1e-4, err
+
+
+@pytest.mark.parametrize("n_", [1, 2, 255, 256, 257, 511, 512, 513, 1025])
+def test_ragged_particle_counts(n_):
+    """Particle counts around the chunk size (512 = two particles per thread of a 256-thread CTA)
+    through the resident solver (fused G2P + P2G, re-sort every 3 substeps) against the in-place
+    substeps, float64."""
+    rng = np.random.default_rng(n_)
+    res, dt, g, steps = 16, 2e-4, -9.8, 7
+    x = rng.uniform(0.3, 0.7, (n_, 3))
+    v = rng.normal(0, 0.5, (n_, 3))
+    vol = 1e-5
+    mu, lam = 300.0, 500.0
+    solver = MPMSolver(torch.tensor(x), res=res, dt=dt, gravity=g, volume=vol, mass=vol, mu_0=mu, lambda_0=lam,
+                       v=torch.tensor(v), dtype=torch.float64, sort_every=3)
+    solver.step(steps, check=True)
+    got = solver.state()
+    dt64 = torch.float64
+    ps = ParticleSet(t(x, dt64), t(np.full(n_, vol), dt64), t(np.full(n_, mu), dt64), t(np.full(n_, lam), dt64))
+    vv, F, C, Jp = mls_mpm.make_mls_mpm_coefficients(n_, 3, dtype=dt64)
+    vv.copy_(t(v, dt64))
+    for _ in range(steps):
+        mls_mpm.solve_mls_mpm_3d(res, float(res), 1.0, 1 / res, dt, vol, g, ps, vv, F, C, Jp)
+    close(n(got["x"]), n(ps.pos), 1e-12, scale=1.0, what="x")
+    close(n(got["v"]), n(vv), 1e-10, scale=max(float(np.abs(v).max()), 1.0), what="v")
+    close(n(got["F"]), n(F), 1e-11, scale=1.0, what="F")
+    close(n(got["C"]), n(C), 1e-9, scale=max(float(np.abs(n(C)).max()), 1.0), what="C")
