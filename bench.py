@@ -164,7 +164,10 @@ def run_ours(args):
     info = solver.plan_info()
     solver.step(args.warmup)
     torch.cuda.synchronize(dev)
-    gsteps = 10 if args.steps % 10 == 0 else 2
+    # substeps per captured CUDA graph: a multiple of the re-sort cadence where the step count allows
+    # (every call starts with a sort, so a graph of 40 re-sorts exactly every 8 substeps, a graph of
+    # 10 at substeps 0 and 8 of every call)
+    gsteps = next((c for c in (5 * SORT_EVERY, 2 * SORT_EVERY, SORT_EVERY, 10, 2) if args.steps % c == 0), 2)
     if args.steps % gsteps == 0:
         solver.capture(gsteps)
 
@@ -215,7 +218,7 @@ def run_ours(args):
     # x, F, ids and the node velocities (12 B), writes x, F, ids, adds 16 B per node, and writes the
     # next key only on the launch before a re-sort (1 of the 9 fused launches of a 10-substep call
     # that re-sorts every 8)
-    key_frac = ((gsteps - 2) // SORT_EVERY) / max(gsteps - 1, 1)
+    key_frac = ((gsteps - 2) // SORT_EVERY) / max(gsteps - 1, 1)  # fused launches that write keys
     alg = {"p2g": n * 96 + active * 16, "g2p": n * 144 + active * 12,
            "g2p2g": int(n * (104 + 4 * key_frac)) + active * 28}
     alg = {k: v for k, v in alg.items() if k in phase_ms}

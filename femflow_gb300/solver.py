@@ -52,7 +52,9 @@ class MPMSolver:
     (``mass``, ``mu_0``, ``lambda_0`` tensors) or scalar.  ``sort_every``: substeps between re-sorts
     by block (with separate G2P and P2G launches a particle that leaves the blocks around its own
     triggers an earlier one; the fused path handles such particles in place; the deterministic mode
-    re-sorts every substep).  ``planes``: up to 8 planar colliders (point, normal) that every grid
+    re-sorts every substep).  Every ``step`` call (and every replay of a captured graph) starts with
+    a sort, so calls whose length is a multiple of ``sort_every`` re-sort exactly every
+    ``sort_every`` substeps.  ``planes``: up to 8 planar colliders (point, normal) that every grid
     update applies (three_d/grid_op.py:50-67; ``plane_rule`` "sticky" or "reference_literal").
     """
 
