@@ -21,6 +21,11 @@ namespace {
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// The Python mirror (_native.Params / Particles, ctypes) relies on these layouts; its test checks
+// the same sizes.
+static_assert(sizeof(ffmpm_params) == 496, "ffmpm_params layout");
+static_assert(sizeof(ffmpm_particles) == 80, "ffmpm_particles layout");
+
 int ilog2_ceil(int64_t v) {
   int b = 0;
   while ((int64_t(1) << b) < v) ++b;

@@ -11,6 +11,12 @@ from femflow_gb300.solvers.mpm import particle as PT
 from femflow_gb300.solvers.mpm import utils as U
 
 
+def test_abi_struct_sizes():
+    """The ctypes mirrors have the sizes the library is compiled against (static_assert in capi.cu)."""
+    assert ctypes.sizeof(N.Params) == 496
+    assert ctypes.sizeof(N.Particles) == 80
+
+
 def test_params_packing():
     p = E.make_params(3, 64, torch.float64, 1 / 64, 64.0, 1e-4, -9.8, 2e-6, 1.0, model="snow", wall_mode="sticky3")
     assert (p.dim, p.res, p.real_bytes, p.model, p.wall_mode) == (3, 64, 8, 1, 1)
