@@ -134,3 +134,40 @@ def test_adjoint_through_a_collider_matches_central_differences():
     eps = 1e-5
     fd = (float(loss(v0 + eps * direction)) - float(loss(v0 - eps * direction))) / (2 * eps)
     assert abs(ad - fd) <= 1e-6 * max(abs(fd), 1e-12), (ad, fd)
+
+
+def test_2d_solver_planes_match_per_phase_composition():
+    """2D resident solver with a plane against two_d.p2g -> grid_op -> the collider -> g2p (float64;
+    x and v: 2D F is defined up to the sign of LAPACK's SVD, two_d/g2p.py:37-43)."""
+    from femflow_gb300.solvers.mpm import two_d
+
+    rng = np.random.default_rng(12)
+    n, res, dt, g, steps = 2000, 48, 2e-4, -9.8, 30
+    x = rng.uniform(-0.06, 0.06, (n, 2)) + [0.5, 0.40]
+    v = np.tile([[0.3, -3.0]], (n, 1))
+    vol = 0.12 ** 2 / n
+    E_, nu = 3e3, 0.3
+    mu, lam = E_ / (2 * (1 + nu)), E_ * nu / ((1 + nu) * (1 - 2 * nu))
+    planes = [((0.5, 0.33), (0.15, 1.0))]
+    solver = MPMSolver(torch.tensor(x), res=res, dt=dt, gravity=g, volume=vol, mass=vol, mu_0=mu, lambda_0=lam,
+                       v=torch.tensor(v), dtype=torch.float64, planes=planes)
+    solver.step(steps, check=True)
+    got = solver.state()
+    t = lambda a: torch.tensor(a, dtype=torch.float64, device="cuda")
+    gx, gvv = t(x), t(v)
+    gF, gC, gJ = t(np.tile(np.eye(2), (n, 1, 1))), t(np.zeros((n, 2, 2))), t(np.ones((n, 1)))
+    R = res + 1
+    prm = E.make_params(2, res, torch.float64, 1 / res, float(res), dt, plane_rule="sticky")
+    pts = np.ascontiguousarray([p for p, _ in planes], dtype=np.float64)
+    nrm = np.ascontiguousarray([q for _, q in planes], dtype=np.float64)
+    for _ in range(steps):
+        gv = torch.zeros((R, R, 2), dtype=torch.float64, device="cuda")
+        gm = torch.zeros((R, R, 1), dtype=torch.float64, device="cuda")
+        two_d.p2g(float(res), 1.0, mu, lam, vol, 1 / res, dt, vol, gv, gm, gx, gvv, gF, gC, gJ)
+        two_d.grid_op(res, dt, g, gv, gm)
+        N.call("ffmpm_check_collision_points", ctypes.byref(prm), pts.ctypes.data_as(ctypes.c_void_p),
+               nrm.ctypes.data_as(ctypes.c_void_p), 1, ctypes.c_void_p(gv.data_ptr()),
+               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        two_d.g2p(float(res), dt, gv, gx, gvv, gF, gC, gJ)
+    np.testing.assert_allclose(got["x"].cpu().numpy(), gx.cpu().numpy(), rtol=0, atol=1e-12)
+    np.testing.assert_allclose(got["v"].cpu().numpy(), gvv.cpu().numpy(), rtol=0, atol=1e-9)
