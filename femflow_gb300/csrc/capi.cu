@@ -315,6 +315,25 @@ size_t tile_smem(const Layout& L) {
   return size_t(tn) * 4 * sizeof(T);
 }
 
+// Dynamic shared memory every kernel may use (set_smem raises each kernel's limit to it).
+constexpr size_t kMaxDynSmem = 200 * 1024;
+
+// Dynamic shared memory of the cell-run P2G and of the fused G2P + P2G for this layout.
+size_t cells_smem_bytes(const Layout& L) {
+  if (L.real_bytes == 4)
+    return L.dim == 3 ? tile_smem<3, float>(L) + cell_run_smem_bytes<3, float>(L.bs)
+                      : tile_smem<2, float>(L) + cell_run_smem_bytes<2, float>(L.bs);
+  return L.dim == 3 ? tile_smem<3, double>(L) + cell_run_smem_bytes<3, double>(L.bs)
+                    : tile_smem<2, double>(L) + cell_run_smem_bytes<2, double>(L.bs);
+}
+
+size_t fused_smem_bytes(const Layout& L) {
+  const int tn = L.dim == 3 ? L.tile * L.tile * L.tile : L.tile * L.tile;
+  if (L.real_bytes == 4)
+    return L.dim == 3 ? g2p2g_smem_bytes<3, float>(tn, L.bs) : g2p2g_smem_bytes<2, float>(tn, L.bs);
+  return L.dim == 3 ? g2p2g_smem_bytes<3, double>(tn, L.bs) : g2p2g_smem_bytes<2, double>(tn, L.bs);
+}
+
 // Raise a kernel's dynamic shared-memory limit once per kernel (a host-side attribute call,
 // kept out of CUDA-graph captures, which run after the first direct call).
 template <typename F>
@@ -324,7 +343,7 @@ void set_smem(F* kernel, size_t bytes) {
   static std::set<const void*> done;
   std::lock_guard<std::mutex> lock(mu);
   if (done.insert(reinterpret_cast<const void*>(kernel)).second)
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDynSmem);
 }
 
 template <int DIM, typename T, typename Sink>
@@ -408,9 +427,11 @@ int launch_g2p2g(const ffmpm_params& p, const Layout& L, const Ws& w, const PVie
 }
 
 // Fused G2P + P2G in the sorted solver: the default outside the deterministic mode and the P2G
-// variants, for runs of two or more substeps.
-bool fused(const ffmpm_params& p, int nsteps) {
-  return !p.deterministic && nsteps >= 2 && (p.variant & (kVariantNoFuse | kVariantP2GDirect | kVariantP2GLanes)) == 0;
+// variants, for runs of two or more substeps whose two tiles and records fit in shared memory.
+bool fused(const ffmpm_params& p, const Layout& L, int nsteps) {
+  return !p.deterministic && nsteps >= 2 &&
+         (p.variant & (kVariantNoFuse | kVariantP2GDirect | kVariantP2GLanes)) == 0 &&
+         fused_smem_bytes(L) <= kMaxDynSmem;
 }
 
 // ------------------------------------------------------------------------------------ operations
@@ -485,7 +506,7 @@ template <int DIM, typename T>
 int op_substeps_sorted(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_particles* a, ffmpm_particles* b,
                        int32_t* ids_a, int32_t* ids_b, int nsteps, cudaStream_t s, PhaseTimer* tm = nullptr) {
   PView<T> va = pview<T>(*a), vb = pview<T>(*b);
-  if (fused(p, nsteps)) return op_substeps_fused<DIM, T>(p, L, w, va, vb, ids_a, ids_b, nsteps, s, tm);
+  if (fused(p, L, nsteps)) return op_substeps_fused<DIM, T>(p, L, w, va, vb, ids_a, ids_b, nsteps, s, tm);
   const int K = sort_every(p);
   const uint32_t* flag = K > 1 ? &w.hdr->sort_now : nullptr;
   for (int k = 0; k < nsteps; ++k) {
@@ -632,7 +653,9 @@ int prologue(const ffmpm_params* p, int64_t n, void* ws, size_t ws_bytes, Layout
     const size_t smem = p->real_bytes == 4 ? (p->dim == 3 ? p2g_det_smem_bytes<3, float>(tn) : p2g_det_smem_bytes<2, float>(tn))
                                            : (p->dim == 3 ? p2g_det_smem_bytes<3, double>(tn)
                                                           : p2g_det_smem_bytes<2, double>(tn));
-    if (smem > 200 * 1024) return FFMPM_ERR_UNSUPPORTED;  // warp tiles + records must fit in shared memory
+    if (smem > kMaxDynSmem) return FFMPM_ERR_UNSUPPORTED;  // warp tiles + records must fit in shared memory
+  } else if (cells_smem_bytes(*L) > kMaxDynSmem) {
+    return FFMPM_ERR_UNSUPPORTED;  // the cell-run P2G's tile and records must fit in shared memory
   }
   if (!ws || ws_bytes < L->total || (reinterpret_cast<uintptr_t>(ws) & 255)) return FFMPM_ERR_WORKSPACE;
   return FFMPM_OK;
@@ -786,7 +809,7 @@ int ffmpm_kernels_per_call(const ffmpm_params* p, int64_t n, int32_t nsteps, int
   const int64_t sort = 1 + L.passes + 3;  // digit histogram, one kernel per pass, three plan kernels
   if (n == 0 || nsteps == 0) {
     *count = 0;
-  } else if (fused(*p, nsteps)) {
+  } else if (fused(*p, L, nsteps)) {
     // keys + sort + P2G; per substep k < n-1: grid update + fused kernel (+ sort when 1 <= k <= n-2
     // is a multiple of the cadence); the last substep: grid update + G2P
     *count = (1 + sort + 1) + int64_t(nsteps - 1) * 2 + int64_t((nsteps - 2) / sort_every(*p)) * sort + 2;

@@ -83,3 +83,33 @@ def test_kernels_per_call():
     assert count(1, variant=every8) == 1 + sort + 3 + 1
     assert count(10, variant=every8 | 4) == 10 * (1 + sort + 3) + 1
     assert count(0, variant=every8) == 0
+
+
+def test_shared_memory_capacity_checks():
+    """3D with 16-node block sides: in float32 the fused kernel's two tiles do not fit in shared
+    memory, so sorted runs keep separate launches; in float64 not even the cell-run P2G fits, and
+    the operations answer FFMPM_ERR_UNSUPPORTED (before any device work)."""
+    every8 = 8 << 8
+
+    def params(dtype, bs):
+        return E.make_params(3, 128, dtype, 1 / 128, 128.0, 1e-4, block_size=bs, variant=every8)
+
+    def count(prm, nsteps):
+        c = ctypes.c_int64()
+        N.call("ffmpm_kernels_per_call", ctypes.byref(prm), 1 << 20, int(nsteps), ctypes.byref(c))
+        return c.value
+
+    info = (ctypes.c_int64 * 8)()
+    N.call("ffmpm_plan_info", ctypes.byref(params(torch.float32, 16)), 1 << 20, info)
+    sort = 1 + info[4] + 3
+    # block side 16 in float32: separate launches (decide, sort, P2G, grid, G2P per substep, keys once)
+    assert count(params(torch.float32, 16), 10) == 10 * (1 + sort + 3) + 1
+    # block side 8: the fused kernel
+    assert count(params(torch.float32, 8), 10) < 10 * (1 + sort + 3) + 1
+    lib = N.load()
+    P = N.Particles()
+    P.n = 16
+    for dtype, want in ((torch.float64, N.ERR_UNSUPPORTED), (torch.float32, N.ERR_WORKSPACE)):
+        prm = params(dtype, 16)
+        rc = lib.ffmpm_substep(ctypes.byref(prm), ctypes.byref(P), None, ctypes.c_size_t(0), None)
+        assert rc == want, (dtype, rc)
