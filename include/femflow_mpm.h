@@ -68,7 +68,10 @@ typedef struct ffmpm_params {
   int32_t model;        /* FFMPM_MODEL_* */
   int32_t wall_mode;    /* FFMPM_WALLS_* */
   int32_t deterministic;/* 1: P2G sums in a fixed order (bit-identical across runs) */
-  int32_t block_size;   /* nodes per block side for work assignment; 0 = default */
+  int32_t block_size;   /* nodes per block side for work assignment, a power of two in 2..16; 0 =
+                         * default (3D 8, 2D 16; deterministic 3D 4, 2D 8).  Sides whose P2G tile
+                         * does not fit in shared memory (3D float64 with 16) answer
+                         * FFMPM_ERR_UNSUPPORTED */
   int32_t variant;      /* kernel variant flags; 0 = default.  Bit 0: P2G scatters straight to the
                          * grid; bit 1: P2G with one shared-memory atomic per (particle, node) (both
                          * with a re-sort every substep); bit 2: ffmpm_substeps_sorted launches G2P
