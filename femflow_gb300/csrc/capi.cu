@@ -62,7 +62,8 @@ bool valid_params(const ffmpm_params* p) {
 }  // namespace
 
 bool make_layout(const ffmpm_params& p, int64_t n, Layout* L) {
-  if (!valid_params(&p) || n < 0 || n > int64_t(0x7FFFFFFF)) return false;
+  // below 2^30 particles: the radix sort's look-back words carry 30-bit counts
+  if (!valid_params(&p) || n < 0 || n >= (int64_t(1) << 30)) return false;
   L->dim = p.dim;
   L->real_bytes = p.real_bytes;
   L->res = p.res;

@@ -116,7 +116,8 @@ typedef struct ffmpm_grid {
 int ffmpm_check_collision_points(const ffmpm_params *p, const double *points, const double *normals, int32_t n,
                                  void *grid_velocity, void *stream);
 
-/* Bytes of workspace needed for `n` particles with these params. */
+/* Bytes of workspace needed for `n` particles with these params (n < 2^30 for every call that
+ * takes a workspace; larger n answers FFMPM_ERR_BADARG). */
 int ffmpm_workspace_size(const ffmpm_params *p, int64_t n, size_t *bytes);
 
 /* Prepare a freshly allocated workspace (zeroes its grids and counters).  Call once. */

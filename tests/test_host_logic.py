@@ -113,3 +113,12 @@ def test_shared_memory_capacity_checks():
         prm = params(dtype, 16)
         rc = lib.ffmpm_substep(ctypes.byref(prm), ctypes.byref(P), None, ctypes.c_size_t(0), None)
         assert rc == want, (dtype, rc)
+
+
+def test_particle_count_limit():
+    """Workspace calls take fewer than 2^30 particles (the sort's look-back words hold 30-bit counts)."""
+    prm = E.make_params(3, 64, torch.float32, 1 / 64, 64.0, 1e-4)
+    out = ctypes.c_size_t(0)
+    lib = N.load()
+    assert lib.ffmpm_workspace_size(ctypes.byref(prm), (1 << 30) - 1, ctypes.byref(out)) == N.OK
+    assert lib.ffmpm_workspace_size(ctypes.byref(prm), 1 << 30, ctypes.byref(out)) == N.ERR_BADARG
