@@ -1230,26 +1230,32 @@ __global__ void __launch_bounds__(kThreads) k_p2g_det(KParams<T> kp, Geom<DIM> g
 #pragma unroll
         for (int i = 0; i < 3; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = T(0);
         if (active) {
-          for (int l = l0 + grp; l < l1; l += NG) {
-            const Node4<T>* src = reinterpret_cast<const Node4<T>*>(recs + (size_t)l * RS);
-            T rv[RS];
-#pragma unroll
-            for (int i = 0; i < (RF + 3) / 4; ++i) {
-              const Node4<T> q4 = src[i];
-              rv[4 * i] = q4.x;
-              rv[4 * i + 1] = q4.y;
-              rv[4 * i + 2] = q4.z;
-              rv[4 * i + 3] = q4.w;
-            }
-            const T m = rv[0];
+          // as in p2g_cell_runs: a lane loads m, q, dx A and the x weights (RU floats) and its own
+          // y (and z) weight; two records per step, added in the same order as one at a time
+          constexpr int RU = DIM == 3 ? 16 : 12;
+          struct Rv {
+            T v[RU];
             T wjk;
-            if constexpr (DIM == 3) {
-              const T wy = oj == 0 ? rv[w0 + 3] : (oj == 1 ? rv[w0 + 4] : rv[w0 + 5]);
-              const T wz = ok == 0 ? rv[w0 + 6] : (ok == 1 ? rv[w0 + 7] : rv[w0 + 8]);
-              wjk = wy * wz;
-            } else {
-              wjk = oj == 0 ? rv[w0 + 3] : (oj == 1 ? rv[w0 + 4] : rv[w0 + 5]);
+          };
+          const auto load = [&](int l, Rv& rv) {
+            const T* rc = recs + (size_t)l * RS;
+            const Node4<T>* src = reinterpret_cast<const Node4<T>*>(rc);
+#pragma unroll
+            for (int i = 0; i < RU / 4; ++i) {
+              const Node4<T> q4 = src[i];
+              rv.v[4 * i] = q4.x;
+              rv.v[4 * i + 1] = q4.y;
+              rv.v[4 * i + 2] = q4.z;
+              rv.v[4 * i + 3] = q4.w;
             }
+            if constexpr (DIM == 3)
+              rv.wjk = rc[w0 + 3 + oj] * rc[w0 + 6 + ok];
+            else
+              rv.wjk = rc[w0 + 3 + oj];
+          };
+          const auto accum = [&](const Rv& r) {
+            const T* rv = r.v;
+            const T m = rv[0];
             T bse[DIM], stp[DIM];
 #pragma unroll
             for (int rr = 0; rr < DIM; ++rr) {
@@ -1260,11 +1266,24 @@ __global__ void __launch_bounds__(kThreads) k_p2g_det(KParams<T> kp, Geom<DIM> g
             }
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
-              const T wgt = rv[w0 + i] * wjk;
+              const T wgt = rv[w0 + i] * r.wjk;
 #pragma unroll
               for (int rr = 0; rr < DIM; ++rr) acc[i][rr] += wgt * (bse[rr] + T(i) * stp[rr]);
               acc[i][3] += wgt * m;
             }
+          };
+          int l = l0 + grp;
+          for (; l + NG < l1; l += 2 * NG) {
+            Rv ra, rb;
+            load(l, ra);
+            load(l + NG, rb);
+            accum(ra);
+            accum(rb);
+          }
+          if (l < l1) {
+            Rv ra;
+            load(l, ra);
+            accum(ra);
           }
         }
 #pragma unroll
