@@ -319,8 +319,8 @@ def run_reference(args):
     t0 = time.perf_counter()
     substep(full)
     t_full = time.perf_counter() - t0
-    budget = 150.0
-    frac = min(1.0, budget / max(1e-9, (args.steps + args.warmup) * t_full))
+    cap_s = 150.0  # seconds of CPU work for the whole run
+    frac = min(1.0, cap_s / max(1e-9, (args.steps + args.warmup) * t_full))
     if frac < 1.0:
         rng = np.random.default_rng(1)
         idx = np.sort(rng.choice(n, size=max(1024, int(n * frac)), replace=False))

@@ -13,7 +13,7 @@ the tensor cores, which adds dF and dv to each particle's result.
 * Rollout: every ``check_every`` coarse steps the range of det F and the total energy (FP64
   diagnostics) are checked; outside det F in [0.5, 2] or an energy gain above ``energy_tol`` the
   segment is discarded and redone with plain fine steps (the fallback).  The plain fine rollout is
-  the judge: positions of the corrected and of the plain coarse rollouts are compared with it.
+  the yardstick: positions of the corrected and of the plain coarse rollouts are compared with it.
 """
 from __future__ import annotations
 
