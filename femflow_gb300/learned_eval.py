@@ -11,7 +11,7 @@
    0 (the network off) is always a candidate, so the selected form is never worse than the plain
    coarse step on the validation scene.
 4. Evaluation on the two-cube scene of 2 x ``--n-per-cube`` particles: plain fine rollout (the
-   judge), plain coarse rollout and the selected corrected rollout with the det F / energy fallback,
+   reference for the error), plain coarse rollout and the selected corrected rollout with the det F / energy fallback,
    each timed end to end on the GPU (synchronised wall clock), for the same simulated time.  The
    fine and the plain coarse forms are also timed on the resident block-sorted solver (all substeps in
    one call; the fastest form of each), and the corrected form runs there too when the selected
