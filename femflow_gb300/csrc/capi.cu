@@ -376,9 +376,10 @@ void launch_p2g_det(const ffmpm_params& p, const Layout& L, const Ws& w, const P
   const size_t smem = p2g_det_smem_bytes<DIM, T>(tn);
   auto kern = k_p2g_det<DIM, T>;
   set_smem(kern, smem);
+  cudaMemsetAsync(w.hdr->det_next, 0, sizeof(w.hdr->det_next), s);  // the CTAs' shared work counters
   kern<<<work_grid(L.nblocks, resident_per_sm(kern, smem)), kThreads, smem, s>>>(
       kparams<T>(p), geom<DIM>(L), P, perm, w.occupied, w.hdr, static_cast<Node4<T>*>(w.stage), &w.hdr->status,
-      &w.hdr->polar_fallbacks);
+      &w.hdr->polar_fallbacks, w.hdr->det_next);
 }
 
 template <int DIM, typename T>

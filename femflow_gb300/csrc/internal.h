@@ -23,7 +23,8 @@ struct WsHeader {
   uint32_t n_valid;
   uint32_t sort_now;   // sort cadence: 1 when this substep re-sorts (set by k_sort_decide)
   uint32_t far_stray;  // set by G2P when a particle left the neighbourhood its block's plan covers
-  uint32_t pad[56];
+  uint32_t det_next[2];  // deterministic P2G: next entry of the occupied list, per pass (zeroed per launch)
+  uint32_t pad[54];
 };
 static_assert(sizeof(WsHeader) == 256, "header is one 256-byte line");
 

@@ -1118,7 +1118,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
 }
 
 // ----------------------------------------------------------------------------------------------
-// Deterministic P2G.  One CTA per occupied block.  Runs (as in k_p2g_cells) go to warps by a fixed
+// Deterministic P2G.  One CTA sums each occupied block.  Runs (as in k_p2g_cells) go to warps by a fixed
 // rule (run r of a chunk -> warp r mod 8) and every warp adds its runs' node sums, in run order,
 // into its own shared tile without atomics; the eight tiles are summed in warp order into the
 // block's staging tile.  The grid update then sums the (at most 2^DIM) staged tiles that cover a
@@ -1135,7 +1135,7 @@ __global__ void __launch_bounds__(kThreads) k_p2g_det(KParams<T> kp, Geom<DIM> g
                                                       const uint32_t* __restrict__ perm,
                                                       const int4* __restrict__ occupied,
                                                       const WsHeader* __restrict__ hdr, Node4<T>* __restrict__ stage,
-                                                      int32_t* status, uint32_t* fallbacks) {
+                                                      int32_t* status, uint32_t* fallbacks, uint32_t* next) {
   constexpr int RF = RecLayout<DIM>::kFloats;
   constexpr int RS = RecLayout<DIM>::kStride;
   constexpr int NW = kThreads / 32;
@@ -1159,8 +1159,23 @@ __global__ void __launch_bounds__(kThreads) k_p2g_det(KParams<T> kp, Geom<DIM> g
   constexpr int a0 = 1 + DIM;
   constexpr int w0 = RecLayout<DIM>::kW;
   const uint32_t nocc = hdr->n_occupied;
-  for (uint32_t ob = blockIdx.x; ob < nocc; ob += gridDim.x) {
+  __shared__ uint32_t next_s;
+  // Blocks go to CTAs through two shared counters (zeroed before the launch): the first pass takes
+  // the blocks of at least two full chunks, the second the rest, so that the large work items
+  // start first and the CTAs finish close together.  Which CTA sums a block changes no sum: each
+  // block is summed by one CTA, in the fixed order below, into its own staging tile.
+  int pass = 0;
+  for (;;) {
+    __syncthreads();  // every thread has read next_s and finished the previous block
+    if (threadIdx.x == 0) next_s = atomicAdd(&next[pass], 1u);
+    __syncthreads();
+    const uint32_t ob = next_s;
+    if (ob >= nocc) {
+      if (++pass == 2) break;
+      continue;
+    }
     const int4 occ = occupied[ob];
+    if ((occ.z >= 2 * kChunk) != (pass == 0)) continue;
     int org[DIM];
     {
       int bc[DIM];
