@@ -216,7 +216,7 @@ def run_ours(args):
     # algorithmic bytes per launch: P2G reads x, v, F, C and adds 16 B per active node; G2P reads x, F,
     # ids and the node velocities and writes x, v, C, F, ids and the next key; the fused G2P + P2G reads
     # x, F, ids and the node velocities (12 B), writes x, F, ids, adds 16 B per node, and writes the
-    # next key only on the launch before a re-sort (1 of the 9 fused launches of a 10-substep call
+    # next key only on the launch before a re-sort (4 of the 39 fused launches of a 40-substep call
     # that re-sorts every 8)
     key_frac = ((gsteps - 2) // SORT_EVERY) / max(gsteps - 1, 1)  # fused launches that write keys
     alg = {"p2g": n * 96 + active * 16, "g2p": n * 144 + active * 12,
