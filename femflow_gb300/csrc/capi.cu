@@ -266,7 +266,7 @@ struct PhaseTimer {
 };
 
 // Substeps between re-sorts (ffmpm_params.variant bits 8..15; 0 or 1: every substep).  The
-// deterministic mode always re-sorts (its per-block CTAs need every particle in its block).
+// deterministic mode always re-sorts (the CTA that sums a block needs every particle in that block).
 int sort_every(const ffmpm_params& p) {
   const int k = (p.variant >> kVariantSortShift) & 0xFF;
   return (p.deterministic || k < 1) ? 1 : k;
