@@ -136,7 +136,6 @@ def run_ours(args):
     import torch
     import torch.distributed as dist
 
-    from femflow_gb300 import engine as E
     from femflow_gb300 import replicas as REP
     from femflow_gb300.solver import MPMSolver
     from femflow_gb300.solvers.mpm import mls_mpm, three_d

@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import json
 import os
-from typing import Callable, Hashable, Iterable, Sequence
+from typing import Callable, Hashable, Sequence
 
 import torch
 

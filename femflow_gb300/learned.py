@@ -28,7 +28,7 @@ import torch
 from . import _native as N
 from . import engine as E
 from . import scenes
-from .diff import pack, unpack
+from .diff import pack
 
 OUT_WEIGHTS = (1.0,) * 12
 
