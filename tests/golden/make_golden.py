@@ -3,7 +3,9 @@
 Run once, in a container that holds the reference checkout (it is not available where the GPU
 tests run, which is why the outputs are committed):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [/root/reference]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <reference checkout>
+
+(or with the checkout's root in the environment variable FEMFLOW_REFERENCE).
 
 numba is not installed, so a no-op ``numba`` module is placed in ``sys.modules`` first: ``njit``,
 ``jit`` and ``experimental.jitclass`` become identity decorators, ``typed.List`` becomes ``list``.
@@ -253,7 +255,12 @@ def make_colliders(ref):
 
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    ref_root = args[0] if args else "/root/reference"
+    if "--only" in sys.argv and args and args[0] == sys.argv[sys.argv.index("--only") + 1]:
+        args = args[1:]
+    ref_root = args[0] if args else os.environ.get("FEMFLOW_REFERENCE")
+    if not ref_root:
+        sys.exit("usage: make_golden.py <reference checkout> [--only colliders] "
+                 "(or set FEMFLOW_REFERENCE to the checkout's root)")
     ref = install_reference(ref_root)
     if "--only" in sys.argv:
         only = sys.argv[sys.argv.index("--only") + 1]

@@ -11,6 +11,7 @@ from oracle import mlp as M
 from femflow_gb300 import _native as N
 from femflow_gb300 import engine as E
 from femflow_gb300 import learned as L
+from femflow_gb300.diff import unpack
 
 pytestmark = pytest.mark.gpu
 
@@ -131,7 +132,7 @@ def test_fused_corrector_matches_unfused_forward():
     c_tol = 1e-6 * 4 * st.res * float(plain[3:6].abs().max())
     assert float((corr[15:24] - plain[15:24]).abs().max()) <= c_tol
     lo, hi = st.det_range()
-    J = torch.linalg.det(L.unpack(corr)[2].double())
+    J = torch.linalg.det(unpack(corr)[2].double())
     assert abs(lo - float(J.min())) < 1e-4 and abs(hi - float(J.max())) < 1e-4
 
 
