@@ -29,6 +29,9 @@ STATUS_OOB = 1
 STATUS_NONFINITE = 2
 STATUS_TIMEOUT = 4
 
+INJECT_LOOKBACK_STALL = 1
+INJECT_BARRIER_ABSENT = 2
+
 MODELS = {"neo_hookean": 0, "snow": 1, "fixed_corotated": 2}
 NPHASES = 7
 PHASES = ("keys", "sort", "plan", "p2g", "grid_update", "g2p", "g2p2g")
@@ -44,6 +47,7 @@ class Params(ctypes.Structure):
         ("volume", ctypes.c_double), ("hardening", ctypes.c_double), ("mass", ctypes.c_double),
         ("mu_0", ctypes.c_double), ("lambda_0", ctypes.c_double),
         ("n_planes", ctypes.c_int32), ("plane_rule", ctypes.c_int32), ("planes", (ctypes.c_double * 6) * 8),
+        ("wait_limit", ctypes.c_uint32), ("inject", ctypes.c_uint32),
     ]
 
 
@@ -105,12 +109,13 @@ _PROTOS = {
                                                      ctypes.c_void_p, ctypes.c_void_p]),
     "ffmpm_plan_info": (ctypes.c_int, [_P(Params), ctypes.c_int64, _P(ctypes.c_int64)]),
     "ffmpm_kernels_per_call": (ctypes.c_int, [_P(Params), ctypes.c_int64, ctypes.c_int32, _P(ctypes.c_int64)]),
-    "ffmpm_sort_by_block_static": (ctypes.c_int, [_P(Params), _vp, ctypes.c_int64, _vp, _vp, _vp]),
+    "ffmpm_sort_by_block_static": (ctypes.c_int, [_P(Params), _vp, ctypes.c_int64, _vp, _vp, _vp, _vp]),
     "ffmpm_batch2d_workspace_size": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32, _P(ctypes.c_size_t)]),
     "ffmpm_batch2d_init": (ctypes.c_int, [_vp, ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_size_t, _vp]),
     "ffmpm_batch2d_substeps": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, _P(Particles), ctypes.c_int32,
                                               ctypes.c_int32, ctypes.c_int32, _vp, ctypes.c_size_t, _vp]),
     "ffmpm_batch2d_status": (ctypes.c_int, [_vp, _P(ctypes.c_int32), _vp]),
+    "ffmpm_batch2d_set_waits": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint32, _vp]),
     "ffmpm_adjoint_workspace_size": (ctypes.c_int, [_P(Params), ctypes.c_int64, _P(ctypes.c_size_t)]),
     "ffmpm_substep_adjoint": (ctypes.c_int, [_P(Params), _P(Particles), _P(Adjoint), _vp, ctypes.c_size_t, _vp]),
     "ffmpm_tc_gemm_bf16": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,

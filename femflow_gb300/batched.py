@@ -118,6 +118,20 @@ class Batch2D:
         self.threads, self.ctas_per_sm = best
         return best, timings
 
+    def reset(self):
+        """Zero the status word, the barrier state and both grids (the scene table is kept).  A
+        batch whose status shows FFMPM_STATUS_TIMEOUT holds a partly accumulated grid: reset it
+        before stepping again."""
+        N.call("ffmpm_batch2d_init", ctypes.c_void_p(ctypes.addressof(self.table)), self.nscenes, self.rb,
+               ctypes.c_void_p(self.ws), ctypes.c_size_t(self.ws_bytes),
+               ctypes.c_void_p(E._stream_ptr(self.device)))
+
+    def set_waits(self, wait_limit: int = 0, inject: int = 0):
+        """Bound of the grid-barrier waits (0: the library default) and N.INJECT_* bits, for tests
+        of the bounded waits; ``reset`` restores both to 0."""
+        N.call("ffmpm_batch2d_set_waits", ctypes.c_void_p(self.ws), int(wait_limit), int(inject),
+               ctypes.c_void_p(E._stream_ptr(self.device)))
+
     def status(self) -> int:
         st = ctypes.c_int32(0)
         N.call("ffmpm_batch2d_status", ctypes.c_void_p(self.ws), ctypes.byref(st),

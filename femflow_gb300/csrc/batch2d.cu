@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 #include <vector>
 
@@ -23,7 +24,7 @@ namespace ffmpm {
 namespace {
 
 constexpr int kMaxScenes = FFMPM_BATCH2D_MAX_SCENES;
-constexpr uint32_t kBarrierSpins = 1u << 24;
+constexpr uint32_t kBarrierSpins = 1u << 24;  // default bound of one grid-barrier wait
 
 struct BatchHeader {
   int32_t status;
@@ -32,7 +33,9 @@ struct BatchHeader {
   int32_t nscenes;
   int64_t total_particles;
   int64_t total_nodes;
-  uint32_t pad[56];
+  uint32_t wait_limit;  // grid-barrier wait bound (0: kBarrierSpins), ffmpm_batch2d_set_waits
+  uint32_t inject;      // FFMPM_INJECT_* bits (tests only)
+  uint32_t pad[54];
 };
 static_assert(sizeof(BatchHeader) == 256, "one 256-byte line");
 
@@ -72,7 +75,7 @@ bool batch_layout(const ffmpm_scene2d* sc, int nscenes, int real_bytes, BatchLay
 
 // Grid-wide barrier with a bounded wait.  Returns false (and raises FFMPM_STATUS_TIMEOUT) if the
 // other CTAs did not arrive in time; the caller then leaves the kernel.
-__device__ __forceinline__ bool grid_barrier(BatchHeader* h, int* s_fail) {
+__device__ __forceinline__ bool grid_barrier(BatchHeader* h, int* s_fail, uint32_t limit) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile uint32_t* genp = &h->barrier_gen;
@@ -86,7 +89,7 @@ __device__ __forceinline__ bool grid_barrier(BatchHeader* h, int* s_fail) {
     } else {
       uint32_t spins = 0;
       while (*genp == gen) {
-        if (++spins > kBarrierSpins) {
+        if (++spins > limit) {
           raise_status(&h->status, FFMPM_STATUS_TIMEOUT);
           *s_fail = 1;
           break;
@@ -158,6 +161,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads) k_batch2d_substep(unsigned c
   }
   if (threadIdx.x == 0) s_fail = 0;
   __syncthreads();
+  const uint32_t limit = h->wait_limit ? h->wait_limit : kBarrierSpins;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   // ---- phase 1: P2G
   for (int64_t gp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gp < ntot; gp += stride) {
@@ -206,7 +210,9 @@ __global__ void __launch_bounds__(kBatchMaxThreads) k_batch2d_substep(unsigned c
       }
     }
   }
-  if (!grid_barrier(h, &s_fail)) return;
+  // (fault injection for tests: CTA 0 never arrives, so the first barrier can only end by running out)
+  if ((h->inject & FFMPM_INJECT_BARRIER_ABSENT) && blockIdx.x == 0) return;
+  if (!grid_barrier(h, &s_fail, limit)) return;
   // ---- phase 2: grid update, every node of every scene
   for (int64_t gn = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gn < nnodes; gn += stride) {
     const int si = find_scene(s_noff, nscenes, gn);
@@ -221,7 +227,7 @@ __global__ void __launch_bounds__(kBatchMaxThreads) k_batch2d_substep(unsigned c
     B[gn] = Node4<T>{vel[0], vel[1], T(0), a.w};
     A[gn] = Node4<T>{T(0), T(0), T(0), T(0)};
   }
-  if (!grid_barrier(h, &s_fail)) return;
+  if (!grid_barrier(h, &s_fail, limit)) return;
   // ---- phase 3: G2P
   for (int64_t gp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gp < ntot; gp += stride) {
     const int si = find_scene(s_poff, nscenes, gp);
@@ -291,9 +297,11 @@ __global__ void __launch_bounds__(kBatchMaxThreads) k_batch2d_substep(unsigned c
     }
     const T det = (Fn[0] * Fn[3] - Fn[1] * Fn[2]) + T(1e-10);
     P.Jp[p] = ffclamp(P.Jp[p] * oldJ / det, T(0.6), T(20.0));
+    const T xn[2] = {xp[0] + kp.dt * v[0], xp[1] + kp.dt * v[1]};
+    if (nonfinite_probe(xn, 2) + nonfinite_probe(Fn, 4) != T(0)) raise_status(&h->status, FFMPM_STATUS_NONFINITE);
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
-      P.x[P.at(p, d, 2)] = xp[d] + kp.dt * v[d];
+      P.x[P.at(p, d, 2)] = xn[d];
       P.v[P.at(p, d, 2)] = v[d];
     }
 #pragma unroll
@@ -369,6 +377,9 @@ int ffmpm_batch2d_substeps(int32_t nscenes, int32_t real_bytes, ffmpm_particles*
     if (ctas_per_sm > 0) per_sm = std::min(per_sm, (int)ctas_per_sm);
     const int grid = per_sm * sm_count();  // every CTA resident: the cooperative launch checks it
     unsigned char* wsp = static_cast<unsigned char*>(ws);
+    // a launch whose barrier ran out leaves its arrivals counted: start every call from zero
+    if (cudaMemsetAsync(wsp + offsetof(BatchHeader, barrier_count), 0, sizeof(uint32_t), s) != cudaSuccess)
+      return FFMPM_ERR_CUDA;
     int ns = nscenes;
     void* args[] = {&wsp, &view, &ns};
     cudaLaunchConfig_t cfg = {};
@@ -405,6 +416,16 @@ int ffmpm_batch2d_substeps(int32_t nscenes, int32_t real_bytes, ffmpm_particles*
   v.Jp = static_cast<double*>(P->Jp);
   v.soa = P->stride;
   return launch(k_batch2d_substep<double>, v);
+}
+
+int ffmpm_batch2d_set_waits(void* ws, uint32_t wait_limit, uint32_t inject, void* stream) {
+  if (!ws) return FFMPM_ERR_BADARG;
+  const uint32_t v[2] = {wait_limit, inject};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (cudaMemcpyAsync(static_cast<unsigned char*>(ws) + offsetof(BatchHeader, wait_limit), v, sizeof(v),
+                      cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return FFMPM_ERR_CUDA;
+  return cudaStreamSynchronize(s) == cudaSuccess ? FFMPM_OK : FFMPM_ERR_CUDA;
 }
 
 int ffmpm_batch2d_status(void* ws, int32_t* status, void* stream) {

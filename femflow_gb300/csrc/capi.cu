@@ -23,7 +23,7 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // The Python mirror (_native.Params / Particles, ctypes) relies on these layouts; its test checks
 // the same sizes.
-static_assert(sizeof(ffmpm_params) == 496, "ffmpm_params layout");
+static_assert(sizeof(ffmpm_params) == 504, "ffmpm_params layout");
 static_assert(sizeof(ffmpm_particles) == 80, "ffmpm_particles layout");
 
 int ilog2_ceil(int64_t v) {
@@ -298,7 +298,7 @@ void sort_and_plan(const ffmpm_params& p, const Layout& L, const Ws& w, const PV
   const uint32_t* ks = nullptr;
   if (tm) tm->begin(1);
   radix_sort(w.keys_next, n, L.passes, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, &w.hdr->status, s,
-             &ks, perm, flag);
+             &ks, perm, flag, p.wait_limit, p.inject);
   if (tm) tm->end(1 + L.passes);
   if (tm) tm->begin(2);
   const int ncta = (int)((L.nblocks + kPlanCta - 1) / kPlanCta);
@@ -592,7 +592,8 @@ int op_sort(const ffmpm_params& p, const Layout& L, const Ws& w, const void* x, 
   k_keys<DIM, T><<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(kp, g, xv, n, L.cell_bits, w.keys_next, nullptr,
                                                                      &w.hdr->status);
   const uint32_t *ks = nullptr, *perm = nullptr;
-  radix_sort(w.keys_next, n, L.passes, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, &w.hdr->status, s, &ks, &perm);
+  radix_sort(w.keys_next, n, L.passes, w.keys0, w.keys1, w.vals0, w.vals1, w.hist, (int)L.ntiles, &w.hdr->status, s, &ks,
+             &perm, nullptr, p.wait_limit, p.inject);
   if (keys_out) cudaMemcpyAsync(keys_out, ks, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
   if (perm_out) cudaMemcpyAsync(perm_out, perm, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
   return check_launch();

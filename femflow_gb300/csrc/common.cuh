@@ -49,6 +49,23 @@ __device__ __forceinline__ void raise_status(int32_t* status, int32_t bit) {
   if (status) atomicOr(status, bit);
 }
 
+// NaN when any of the n values is NaN or infinite, else 0: v * 0 is exact for finite v, so no
+// finite value, however large, gives a false alarm.
+template <typename T>
+__device__ __forceinline__ T nonfinite_probe(const T* v, int n) {
+  T acc = T(0);
+#pragma unroll
+  for (int i = 0; i < n; ++i) acc = fma(v[i], T(0), acc);
+  return acc;
+}
+
+// True once a bounded wait has given up (since the status word was last cleared).  A permutation
+// made by a sort that gave up may hold indices the sort never wrote, so kernels that read particles
+// through one leave at once instead.
+__device__ __forceinline__ bool wait_gave_up(const int32_t* status) {
+  return status && (*reinterpret_cast<const volatile int32_t*>(status) & FFMPM_STATUS_TIMEOUT);
+}
+
 // ----------------------------------------------------------------------------------------------
 // Grid geometry shared by all kernels.  Nodes per axis R = res + 1.  The grid is split into
 // cubic (square in 2D) blocks of BS nodes per axis for work assignment: a particle belongs to the

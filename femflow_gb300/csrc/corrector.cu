@@ -319,7 +319,12 @@ __global__ void __launch_bounds__(kThreadsC) k_corrector(KParams<float> kp, cons
     // the next tile rewrites sX / sH: every thread is past this tile's MMAs and reads
     __syncthreads();
   }
-  if (s_fail && tid == 0) raise_status(status, FFMPM_STATUS_TIMEOUT);
+  if (s_fail && tid == 0) {
+    raise_status(status, FFMPM_STATUS_TIMEOUT);
+    // the MMAs of the last commit may still be running: wait for them once more (bounded) before
+    // their tensor memory is freed
+    mbar_wait(&bar, phase ^ 1u);
+  }
   if (det_keys) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {

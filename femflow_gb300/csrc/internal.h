@@ -45,11 +45,13 @@ int sm_count();
 // Radix sort (sort.cu): stable, 8-bit digits, `passes` passes over keys_in (n keys); values start
 // as the identity permutation.  `scratch` holds radix_scratch_words(passes, ntiles) words (zeroed
 // by the call).  Returns the buffers that hold the sorted keys / permutation.  With `sort_flag`
-// (device word, nullable) the kernels do nothing when it reads 0.
+// (device word, nullable) the kernels do nothing when it reads 0.  `wait_limit` bounds each tile's
+// look-back wait (0: the default); `inject` takes FFMPM_INJECT_LOOKBACK_STALL (tests only).
 constexpr int kMaxRadixPasses = 4;
 size_t radix_scratch_words(int passes, int64_t ntiles);
 void radix_sort(const uint32_t* keys_in, uint32_t n, int passes, uint32_t* keys0, uint32_t* keys1, uint32_t* vals0,
                 uint32_t* vals1, uint32_t* scratch, int ntiles, int32_t* status, cudaStream_t s,
-                const uint32_t** keys_sorted, const uint32_t** perm, const uint32_t* sort_flag = nullptr);
+                const uint32_t** keys_sorted, const uint32_t** perm, const uint32_t* sort_flag = nullptr,
+                uint32_t wait_limit = 0, uint32_t inject = 0);
 
 }  // namespace ffmpm

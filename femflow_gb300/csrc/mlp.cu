@@ -86,7 +86,12 @@ __global__ void __launch_bounds__(kGemmThreads) k_tc_gemm(const uint16_t* __rest
     if (s_fail) break;
   }
   if (s_fail) {
-    if (tid == 0 && status) raise_status(status, FFMPM_STATUS_TIMEOUT);
+    if (tid == 0) {
+      if (status) raise_status(status, FFMPM_STATUS_TIMEOUT);
+      // the MMAs of the last commit may still be running: wait for them once more (bounded) before
+      // their tensor memory is freed
+      mbar_wait(&bar, phase ^ 1u);
+    }
   } else if (issued) {
     const int row = m0 + 32 * warp + lane;
 #pragma unroll 1

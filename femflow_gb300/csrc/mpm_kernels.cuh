@@ -1062,6 +1062,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_p2g_cells(
                                                         const WsHeader* __restrict__ hdr, Sink sink, int32_t* status,
                                                         uint32_t* fallbacks, const uint32_t* __restrict__ sort_flag) {
   if (sort_flag && *sort_flag == 0u) perm = nullptr;  // plan kept from an earlier substep: identity order
+  if (perm && wait_gave_up(status)) return;
   constexpr int RS = RecLayout<DIM>::kStride;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int TN = tile_nodes<DIM>(g);
@@ -1136,6 +1137,7 @@ __global__ void __launch_bounds__(kThreads) k_p2g_det(KParams<T> kp, Geom<DIM> g
                                                       const int4* __restrict__ occupied,
                                                       const WsHeader* __restrict__ hdr, Node4<T>* __restrict__ stage,
                                                       int32_t* status, uint32_t* fallbacks, uint32_t* next) {
+  if (wait_gave_up(status)) return;
   constexpr int RF = RecLayout<DIM>::kFloats;
   constexpr int RS = RecLayout<DIM>::kStride;
   constexpr int NW = kThreads / 32;
@@ -1356,6 +1358,7 @@ __global__ void __launch_bounds__(kThreads) k_p2g(KParams<T> kp, Geom<DIM> g, PV
                                                   const uint32_t* __restrict__ perm, const int4* __restrict__ chunks,
                                                   const WsHeader* __restrict__ hdr, Sink sink, int32_t* status,
                                                   uint32_t* fallbacks) {
+  if (wait_gave_up(status)) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   T* tile = reinterpret_cast<T*>(smem_raw);
   const int TN = tile_nodes<DIM>(g);
@@ -1793,6 +1796,9 @@ __device__ __forceinline__ bool g2p_particle(const KParams<T>& kp, const Geom<DI
   T xn[DIM];
 #pragma unroll
   for (int d = 0; d < DIM; ++d) xn[d] = xp[d] + kp.dt * v[d];
+  // a non-finite v reaches x and a non-finite C reaches F (C F has a NaN in that row even where F is
+  // zero), so x and F cover the whole updated state
+  if (nonfinite_probe(xn, DIM) + nonfinite_probe(Fn, DD) != T(0)) raise_status(status, FFMPM_STATUS_NONFINITE);
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     Pout.x[Pout.at(q, d, DIM)] = xn[d];
@@ -1862,6 +1868,7 @@ __global__ void __launch_bounds__(kThreads) k_g2p(KParams<T> kp, Geom<DIM> g, PV
                                                   const T* __restrict__ user_gv, G2PExtra ex, int32_t* status,
                                                   const uint32_t* __restrict__ sort_flag) {
   if (sort_flag && *sort_flag == 0u) perm = nullptr;  // plan kept from an earlier substep: identity order
+  if (perm && wait_gave_up(status)) return;
   // Dynamic shared memory: [pad to 128 B][tile: TN Node4][mbarrier].  The TMA destination must
   // be 128-byte aligned, so the tile start is rounded up explicitly.
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -1905,11 +1912,17 @@ __global__ void __launch_bounds__(kThreads) k_g2p(KParams<T> kp, Geom<DIM> g, PV
         if (!mbar_wait(&bar, phase)) {
           timed_out = true;
         }
-        phase ^= 1u;
         if (__syncthreads_or(timed_out)) {
-          raise_status(status, FFMPM_STATUS_TIMEOUT);
+          // the tile copy may still be in flight: wait for it once more (bounded) so that it does
+          // not land in shared memory after this CTA has left
+          if (threadIdx.x == 0) {
+            raise_status(status, FFMPM_STATUS_TIMEOUT);
+            mbar_wait(&bar, phase);
+          }
+          __syncthreads();
           return;
         }
+        phase ^= 1u;
       } else {
         const int T1 = g.tile;
         for (int t = threadIdx.x; t < TN; t += blockDim.x) {
@@ -2007,6 +2020,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_g2p2g(
     InternalSink<T> sink, uint32_t* __restrict__ tmark, uint32_t* __restrict__ touched, int32_t* status,
     uint32_t* fallbacks, const uint32_t* __restrict__ sort_flag) {
   if (sort_flag && *sort_flag == 0u) perm = nullptr;  // plan kept from an earlier substep: identity order
+  if (perm && wait_gave_up(status)) return;
   constexpr int RS = RecLayout<DIM>::kStride;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int TN = tile_nodes<DIM>(g);
@@ -2056,11 +2070,17 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1) k_g2p2g(
       }
       for (int t = threadIdx.x; t < 4 * TN; t += blockDim.x) ptile[t] = T(0);
       const bool timed_out = !mbar_wait(&bar, phase);
-      phase ^= 1u;
       if (__syncthreads_or(timed_out)) {
-        raise_status(status, FFMPM_STATUS_TIMEOUT);
+        // the tile copy may still be in flight: wait for it once more (bounded) so that it does not
+        // land in shared memory after this CTA has left
+        if (threadIdx.x == 0) {
+          raise_status(status, FFMPM_STATUS_TIMEOUT);
+          mbar_wait(&bar, phase);
+        }
+        __syncthreads();
         return;
       }
+      phase ^= 1u;
     }
     // phase 1: G2P of substep k, then the record of substep k+1, one particle per thread
     for (int l = threadIdx.x; l < ch.z; l += blockDim.x) {

@@ -6,7 +6,11 @@
 // with __match_any_sync in index order, publishes its per-digit counts, and obtains the counts of
 // all earlier tiles by decoupled look-back: it walks back over its predecessors' published words
 // until it meets one that already carries an inclusive prefix.  Every wait is bounded; a tile whose
-// wait runs out skips its scatter and raises FFMPM_STATUS_TIMEOUT instead of hanging.
+// wait runs out skips its scatter and raises FFMPM_STATUS_TIMEOUT instead of hanging.  It still
+// publishes the (partial, hence too small) prefix it has, so that its successors finish: their
+// positions stay below the true ones and inside [0, n).  A pass that starts with the timeout bit
+// already raised does nothing: its input keys were not all written by the previous pass, so their
+// digits need not match the histogram the positions are built from.
 //
 // Stability makes the permutation bit-exact: it equals a CPU stable sort of the same keys (numpy
 // argsort kind="stable").
@@ -30,7 +34,7 @@ static_assert(kRsThreads * kRsItems == kRadixTile, "tile size");
 constexpr uint32_t kFlagAggregate = 1u << 30;
 constexpr uint32_t kFlagInclusive = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
-constexpr uint32_t kLookbackSpins = 1u << 22;
+constexpr uint32_t kLookbackSpins = 1u << 22;  // default bound of one tile's look-back wait
 constexpr int kLookbackBatch = 8;  // predecessor words read per look-back step
 
 // Digit histograms of all passes (ghist[pass][256]), one read of the keys.  Nearly sorted keys put
@@ -81,8 +85,11 @@ __global__ void __launch_bounds__(kRsThreads) k_radix_onesweep(const uint32_t* _
                                                                 uint32_t* __restrict__ tile_counter,
                                                                 uint32_t* __restrict__ keys_out,
                                                                 uint32_t* __restrict__ vals_out, int32_t* status,
-                                                                const uint32_t* __restrict__ sort_flag) {
+                                                                const uint32_t* __restrict__ sort_flag,
+                                                                uint32_t wait_limit, uint32_t inject) {
   if (sort_flag && *sort_flag == 0u) return;
+  // an earlier pass gave up: this pass's input is incomplete
+  if (status && (*reinterpret_cast<const volatile int32_t*>(status) & FFMPM_STATUS_TIMEOUT)) return;
   __shared__ uint32_t wcnt[kRsWarps][256];
   __shared__ uint32_t base[256];
   __shared__ uint32_t warp_sums[kRsWarps];
@@ -158,7 +165,9 @@ __global__ void __launch_bounds__(kRsThreads) k_radix_onesweep(const uint32_t* _
     uint32_t* mine = lookback + (size_t)tile * 256 + d;
     uint32_t excl = 0;
     if (tile == 0) {
-      st_volatile(mine, kFlagInclusive | run);
+      // (fault injection for tests: the first tile never publishes, so every look-back that
+      // reaches it can only end by running out)
+      if (!(inject & FFMPM_INJECT_LOOKBACK_STALL)) st_volatile(mine, kFlagInclusive | run);
     } else {
       st_volatile(mine, kFlagAggregate | run);
       // walk back over the predecessors kLookbackBatch words at a time (the loads of a batch are
@@ -186,7 +195,7 @@ __global__ void __launch_bounds__(kRsThreads) k_radix_onesweep(const uint32_t* _
         if (found) break;
         t -= used;
         if (used == 0) {
-          if (++spins > kLookbackSpins) {
+          if (++spins > wait_limit) {
             s_timeout = 1;
             break;
           }
@@ -204,8 +213,8 @@ __global__ void __launch_bounds__(kRsThreads) k_radix_onesweep(const uint32_t* _
   }
 #pragma unroll
   for (int r = 0; r < kRsItems; ++r) {
-    if (dig[r] < 256u) {
-      const uint32_t pos = base[dig[r]] + wcnt[warp][dig[r]] + off[r];
+    const uint32_t pos = base[dig[r] & 255u] + wcnt[warp][dig[r] & 255u] + off[r];
+    if (dig[r] < 256u && pos < n) {
       if (keys_out) keys_out[pos] = key[r];
       vals_out[pos] = val[r];
     }
@@ -221,7 +230,9 @@ size_t radix_scratch_words(int passes, int64_t ntiles) {
 
 void radix_sort(const uint32_t* keys_in, uint32_t n, int passes, uint32_t* keys0, uint32_t* keys1, uint32_t* vals0,
                 uint32_t* vals1, uint32_t* scratch, int ntiles, int32_t* status, cudaStream_t s,
-                const uint32_t** keys_sorted, const uint32_t** perm, const uint32_t* sort_flag) {
+                const uint32_t** keys_sorted, const uint32_t** perm, const uint32_t* sort_flag, uint32_t wait_limit,
+                uint32_t inject) {
+  if (wait_limit == 0) wait_limit = kLookbackSpins;
   uint32_t* ghist = scratch;                    // [passes][256]
   uint32_t* counters = ghist + 256 * passes;    // [passes], 32-word padded
   uint32_t* lookback = counters + 32 * passes;  // [passes][ntiles][256]
@@ -235,7 +246,8 @@ void radix_sort(const uint32_t* keys_in, uint32_t n, int passes, uint32_t* keys0
   for (int pass = 0; pass < passes; ++pass) {
     k_radix_onesweep<<<ntiles, kRsThreads, 0, s>>>(kin, vin, n, 8 * pass, ghist + 256 * pass,
                                                    lookback + (size_t)pass * ntiles * 256, counters + 32 * pass,
-                                                   kbuf[pass & 1], vbuf[pass & 1], status, sort_flag);
+                                                   kbuf[pass & 1], vbuf[pass & 1], status, sort_flag, wait_limit,
+                                                   inject);
     kin = kbuf[pass & 1];
     vin = vbuf[pass & 1];
   }

@@ -37,10 +37,13 @@ def real_bytes(dtype) -> int:
 def make_params(dim: int, res: int, dtype, dx: float, inv_dx: float, dt: float, gravity: float = 0.0,
                 volume: float = 1.0, hardening: float = 1.0, mass: float = 0.0, mu_0: float = 0.0,
                 lambda_0: float = 0.0, model="neo_hookean", wall_mode="reference", deterministic: bool = False,
-                block_size: int = 0, variant: int = 0, planes=None, plane_rule="sticky") -> N.Params:
+                block_size: int = 0, variant: int = 0, planes=None, plane_rule="sticky", wait_limit: int = 0,
+                inject: int = 0) -> N.Params:
     """Kernel parameters.  ``planes``: up to 8 planar colliders as (point, normal) pairs of ``dim``
     numbers each, applied by every grid update (``plane_rule`` "sticky" or "reference_literal",
-    see ffmpm_params in include/femflow_mpm.h)."""
+    see ffmpm_params in include/femflow_mpm.h).  ``wait_limit`` bounds the sort's look-back wait
+    (0: the library default) and ``inject`` takes N.INJECT_* bits; both are for tests of the
+    bounded waits."""
     p = N.Params()
     p.dim, p.res, p.real_bytes = int(dim), int(res), real_bytes(dtype)
     p.model = N.MODELS[model] if isinstance(model, str) else int(model)
@@ -54,6 +57,7 @@ def make_params(dim: int, res: int, dtype, dx: float, inv_dx: float, dt: float, 
         raise ValueError(f"at most {N.MAX_PLANES} planes")
     p.n_planes = len(planes)
     p.plane_rule = N.PLANE_RULES[plane_rule] if isinstance(plane_rule, str) else int(plane_rule)
+    p.wait_limit, p.inject = int(wait_limit), int(inject)
     for q, (point, normal) in enumerate(planes):
         point, normal = np.asarray(point, dtype=np.float64), np.asarray(normal, dtype=np.float64)
         if point.shape != (dim,) or normal.shape != (dim,):
@@ -94,9 +98,22 @@ class Workspace:
         st, _ = self.status()
         if st:
             self.clear_status()
-            if st & N.STATUS_OOB:
-                raise RuntimeError("particle out of grid bounds (reference: RuntimeError in utils.oob)")
-            raise RuntimeError(f"device status {st:#x}")
+            raise RuntimeError(status_message(st))
+
+
+def status_message(st: int) -> str:
+    """What the FFMPM_STATUS_* bits of a status word report, most specific first."""
+    parts = []
+    if st & N.STATUS_OOB:
+        parts.append("particle out of grid bounds (reference: RuntimeError in utils.oob)")
+    if st & N.STATUS_NONFINITE:
+        parts.append("non-finite value in the particle state (x, v, F or C)")
+    if st & N.STATUS_TIMEOUT:
+        parts.append("a bounded device wait expired; the results of the call are not valid")
+    rest = st & ~(N.STATUS_OOB | N.STATUS_NONFINITE | N.STATUS_TIMEOUT)
+    if rest or not parts:
+        parts.append(f"device status {st:#x}")
+    return "; ".join(parts)
 
 
 def workspace_for(params: N.Params, n: int, device) -> Workspace:

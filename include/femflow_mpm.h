@@ -42,7 +42,17 @@ extern "C" {
 /* status-word bits (device side, see ffmpm_status_read) */
 #define FFMPM_STATUS_OOB 1       /* particle stencil outside the grid, or non-finite position */
 #define FFMPM_STATUS_NONFINITE 2 /* non-finite value produced in the particle state */
-#define FFMPM_STATUS_TIMEOUT 4   /* a bounded device wait expired (never expected) */
+#define FFMPM_STATUS_TIMEOUT 4   /* a bounded device wait expired (never expected); the results of
+                                  * the call are not valid, and kernels that would index particles
+                                  * through an unfinished sort skip their work until the word is
+                                  * cleared */
+
+/* Fault injection for tests of the bounded waits (ffmpm_params.inject, ffmpm_batch2d_set_waits).
+ * Each makes one wait impossible to satisfy, so that it can only end by running out; 0 in
+ * production. */
+#define FFMPM_INJECT_LOOKBACK_STALL 1 /* radix sort: the first tile of every pass never publishes
+                                       * its digit counts */
+#define FFMPM_INJECT_BARRIER_ABSENT 2 /* batched 2D: CTA 0 leaves before the first grid barrier */
 
 /* material models: reference strings of three_d/p2g.py:57-61 */
 #define FFMPM_MODEL_NEO_HOOKEAN 0 /* "neo_hookean": fixed-corotated stress, constant hardening */
@@ -91,6 +101,11 @@ typedef struct ffmpm_params {
   int32_t n_planes;     /* 0..FFMPM_MAX_PLANES */
   int32_t plane_rule;   /* FFMPM_PLANES_* */
   double planes[FFMPM_MAX_PLANES][6];
+  /* Iterations of the radix sort's look-back wait (a tile waiting for its predecessors' digit
+   * counts) before it gives up and raises FFMPM_STATUS_TIMEOUT; 0 = the default, 2^22 (about a
+   * second).  Lowered only by tests that make the wait run out. */
+  uint32_t wait_limit;
+  uint32_t inject;      /* FFMPM_INJECT_* bits; 0 in production */
 } ffmpm_params;
 
 typedef struct ffmpm_particles {
@@ -196,14 +211,21 @@ int ffmpm_kernels_per_call(const ffmpm_params *p, int64_t n, int32_t nsteps, int
  * five n-sized key/index arrays plus the digit histograms) is one static array in this library,
  * which every GPU that loads the library keeps until the process exits.
  *   - n must be <= FFMPM_STATIC_SORT_MAX_N, otherwise FFMPM_ERR_CAPACITY and nothing runs.
- *   - The first call on a device looks up the array's device address on the current device
- *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - The first call in a CUDA context looks up the array's device address with that context's
+ *     device current (cudaGetSymbolAddress); make that first call before any stream capture.  A
+ *     new context on the device (cudaDeviceReset) makes the next call look the address up again.
  *   - Every call uses the same array, which keeps the previous call's contents: two calls whose
  *     work overlaps on the GPU (different streams or host threads) race and corrupt each other's
  *     results, so serialise them.
+ *   - status_out (device memory, or NULL): receives the call's FFMPM_STATUS_* bits, copied on
+ *     `stream` after the sort — FFMPM_STATUS_OOB when some particle lies outside the grid (it is
+ *     sorted last with key 0xFFFFFFFF; the reference raises RuntimeError for such a particle),
+ *     FFMPM_STATUS_TIMEOUT when a bounded wait of the sort gave up (keys_out and perm_out are then
+ *     not valid).  0 for a clean sort.  The word in the shared array is overwritten by the next
+ *     call, so this copy is the only way to see it.
  * No counterpart in the reference. */
 int ffmpm_sort_by_block_static(const ffmpm_params *p, const void *x, int64_t n, uint32_t *keys_out,
-                               uint32_t *perm_out, void *stream);
+                               uint32_t *perm_out, int32_t *status_out, void *stream);
 
 /* ---- batched 2D scenes: one persistent launch per substep for many independent scenes ---- */
 #define FFMPM_BATCH2D_MAX_SCENES 256
@@ -233,6 +255,13 @@ int ffmpm_batch2d_substeps(int32_t nscenes, int32_t real_bytes, ffmpm_particles 
 
 /* Status word of a batch workspace (FFMPM_STATUS_* bits); synchronises `stream`. */
 int ffmpm_batch2d_status(void *ws, int32_t *status, void *stream);
+
+/* Bound of the grid-barrier waits of a batch (iterations before a CTA gives up, raises
+ * FFMPM_STATUS_TIMEOUT and leaves the launch; 0 = the default, 2^24) and FFMPM_INJECT_* bits
+ * (FFMPM_INJECT_BARRIER_ABSENT), stored in the workspace for the following calls.  Tests lower
+ * the bound to make a barrier run out; a batch whose status shows FFMPM_STATUS_TIMEOUT holds
+ * partial results.  No reference counterpart. */
+int ffmpm_batch2d_set_waits(void *ws, uint32_t wait_limit, uint32_t inject, void *stream);
 
 /* ---- adjoint of one 3D substep (reverse mode, for differentiable rollouts) ---- */
 

@@ -13,7 +13,7 @@ from femflow_gb300.solvers.mpm import utils as U
 
 def test_abi_struct_sizes():
     """The ctypes mirrors have the sizes the library is compiled against (static_assert in capi.cu)."""
-    assert ctypes.sizeof(N.Params) == 496
+    assert ctypes.sizeof(N.Params) == 504
     assert ctypes.sizeof(N.Particles) == 80
 
 
