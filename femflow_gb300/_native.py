@@ -99,6 +99,7 @@ _PROTOS = {
     "ffmpm_grid_op": (ctypes.c_int, [_P(Params), _P(Grid), _vp]),
     "ffmpm_g2p": (ctypes.c_int, [_P(Params), _P(Grid), _P(Particles), _vp, ctypes.c_size_t, _vp]),
     "ffmpm_substep": (ctypes.c_int, [_P(Params), _P(Particles), _vp, ctypes.c_size_t, _vp]),
+    "ffmpm_substep_host": (ctypes.c_int, [_P(Params), _P(Particles), _P(Particles), _vp, ctypes.c_size_t, _vp]),
     "ffmpm_substeps_sorted": (ctypes.c_int, [_P(Params), _P(Particles), _P(Particles), _vp, _vp, ctypes.c_int32,
                                              _vp, ctypes.c_size_t, _vp]),
     "ffmpm_sort_by_block": (ctypes.c_int, [_P(Params), _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_size_t, _vp]),

@@ -454,6 +454,134 @@ int op_substep(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_partic
   return rc != FFMPM_OK ? rc : check_launch();
 }
 
+// ----------------------------------------------------------------------------- host-array substep
+// Copy streams and events of ffmpm_substep_host, one set per device, created by the first call on
+// that device (with it current) and kept until the process exits.
+constexpr int kHostChunks = 4;
+struct HostPipe {
+  cudaStream_t up = nullptr, down = nullptr;
+  cudaEvent_t start = nullptr, gathered_all = nullptr, down_done = nullptr;
+  cudaEvent_t landed[kHostChunks] = {}, gathered[kHostChunks] = {};
+};
+
+int host_pipe(HostPipe** out) {
+  constexpr int kMaxDevices = 64;
+  static std::mutex mu;
+  static HostPipe pipes[kMaxDevices];
+  static bool made[kMaxDevices] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return FFMPM_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(mu);
+  HostPipe& h = pipes[dev];
+  if (!made[dev]) {
+    bool ok = cudaStreamCreateWithFlags(&h.up, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&h.down, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&h.start, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&h.gathered_all, cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&h.down_done, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; ok && k < kHostChunks; ++k)
+      ok = cudaEventCreateWithFlags(&h.landed[k], cudaEventDisableTiming) == cudaSuccess &&
+           cudaEventCreateWithFlags(&h.gathered[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) return FFMPM_ERR_CUDA;
+    made[dev] = true;
+  }
+  *out = &h;
+  return FFMPM_OK;
+}
+
+// One substep on host arrays H through the device arrays D (same shapes, row-major).  Chunk k of
+// every input array goes up on the upload stream and is scattered on `s` once it has landed; after
+// the dense grid update, chunk k is gathered on `s` and its outputs go down on the download stream
+// while chunk k + 1 is gathered.  `s` finally waits for the last download, so that the call is
+// complete, host arrays included, once `s` has run.  (Kernels reading and writing mapped pinned
+// host memory in place measured about 4x slower than this on a GB300: the copy engines, not SM
+// loads and stores, reach the host link's rate here.)
+template <int DIM, typename T>
+int op_substep_host(const ffmpm_params& p, const Layout& L, const Ws& w, const ffmpm_particles* H,
+                    ffmpm_particles* D, cudaStream_t s) {
+  const int64_t n = H->n;
+  HostPipe* hp = nullptr;
+  int rc = host_pipe(&hp);
+  if (rc != FFMPM_OK) return rc;
+  const size_t rb = sizeof(T);
+  struct Arr {
+    void* h;
+    void* d;
+    size_t per;   // bytes per particle
+    bool out;     // written by the substep
+    bool whole;   // one real per particle: sent up whole before the first chunk (fewer, larger copies)
+  };
+  // Jp changes only in 2D and for snow (three_d/g2p.py:48-58): elsewhere it is not sent back
+  const bool jp_out = DIM == 2 || p.model == FFMPM_MODEL_SNOW;
+  const Arr arrs[8] = {{H->x, D->x, DIM * rb, true, false},
+                       {H->v, D->v, DIM * rb, true, false},
+                       {H->F, D->F, DIM * DIM * rb, true, false},
+                       {H->C, D->C, DIM * DIM * rb, true, false},
+                       {H->Jp, D->Jp, rb, jp_out, true},
+                       {const_cast<void*>(H->mass), const_cast<void*>(D->mass), rb, false, true},
+                       {const_cast<void*>(H->mu_0), const_cast<void*>(D->mu_0), rb, false, true},
+                       {const_cast<void*>(H->lambda_0), const_cast<void*>(D->lambda_0), rb, false, true}};
+  // copies of [a, b) of the chunked arrays (whole = false: the per-particle scalars over [0, n))
+  auto copy = [&](bool down, int64_t a, int64_t b, cudaStream_t cs, bool whole = false) {
+    for (const Arr& r : arrs) {
+      if (!r.h || (down && !r.out) || (!down && r.whole != whole)) continue;
+      unsigned char* hb = static_cast<unsigned char*>(r.h) + a * r.per;
+      unsigned char* db = static_cast<unsigned char*>(r.d) + a * r.per;
+      if (down)
+        cudaMemcpyAsync(hb, db, (b - a) * r.per, cudaMemcpyDeviceToHost, cs);
+      else
+        cudaMemcpyAsync(db, hb, (b - a) * r.per, cudaMemcpyHostToDevice, cs);
+    }
+  };
+  // the uploads start after the work already queued on the caller's stream
+  cudaEventRecord(hp->start, s);
+  cudaStreamWaitEvent(hp->up, hp->start, 0);
+  if (p.deterministic) {
+    // the fixed summation order needs the block-sorted path: whole arrays up, ffmpm_substep, down
+    copy(false, 0, n, hp->up, true);
+    copy(false, 0, n, hp->up);
+    cudaEventRecord(hp->landed[0], hp->up);
+    cudaStreamWaitEvent(s, hp->landed[0], 0);
+    rc = op_substep<DIM, T>(p, L, w, D, s);
+    if (rc != FFMPM_OK) return rc;
+    copy(true, 0, n, s);
+    return check_launch();
+  }
+  // Upload chunks shrink (sizes K, K-1, ..., 1) so that little scatter is left once the last one
+  // has landed; gather/download chunks grow (1, 2, ..., K) so that the first download starts soon
+  // after the grid update.
+  const int K = (int)std::max<int64_t>(1, std::min<int64_t>(kHostChunks, (n + 65535) / 65536));
+  const int64_t parts = int64_t(K) * (K + 1) / 2;
+  auto up_lo = [&](int k) { return n * (int64_t(k) * (2 * K - k + 1) / 2) / parts; };
+  auto lo = [&](int k) { return n * (int64_t(k) * (k + 1) / 2) / parts; };
+  const KParams<T> kp = kparams<T>(p);
+  const Geom<DIM> g = geom<DIM>(L);
+  const PView<T> pv = pview<T>(*D);
+  const InternalSink<T> sink{static_cast<Node4<T>*>(w.gridA)};
+  copy(false, 0, n, hp->up, true);
+  for (int k = 0; k < K; ++k) {
+    const int64_t a = up_lo(k), b = up_lo(k + 1);
+    copy(false, a, b, hp->up);
+    cudaEventRecord(hp->landed[k], hp->up);
+    cudaStreamWaitEvent(s, hp->landed[k], 0);
+    k_p2g_range<DIM, T><<<work_grid((b - a + kThreads - 1) / kThreads, 8), kThreads, 0, s>>>(
+        kp, g, pv, (uint32_t)a, (uint32_t)b, sink, &w.hdr->status, &w.hdr->polar_fallbacks);
+  }
+  k_grid_update_dense<DIM, T><<<work_grid((L.nnodes + kThreads - 1) / kThreads, 8), kThreads, 0, s>>>(
+      kp, g, static_cast<Node4<T>*>(w.gridA), static_cast<Node4<T>*>(w.gridB));
+  for (int k = 0; k < K; ++k) {
+    const int64_t a = lo(k), b = lo(k + 1);
+    k_g2p_range<DIM, T><<<work_grid((b - a + kThreads - 1) / kThreads, 8), kThreads, 0, s>>>(
+        kp, g, pv, (uint32_t)a, (uint32_t)b, static_cast<const Node4<T>*>(w.gridB), &w.hdr->status);
+    cudaEventRecord(hp->gathered[k], s);
+    cudaStreamWaitEvent(hp->down, hp->gathered[k], 0);
+    copy(true, a, b, hp->down);
+  }
+  cudaEventRecord(hp->down_done, hp->down);
+  cudaStreamWaitEvent(s, hp->down_done, 0);
+  return check_launch();
+}
+
 // Substeps 0..n-1 with the fused kernel: P2G(0), then for k = 0..n-2: grid update(k), re-sort if
 // due (k a multiple of the cadence), G2P(k) + P2G(k+1); then grid update(n-1) and G2P(n-1).  The
 // state after every substep is in buffer a or b as in the unfused loop (x, F, Jp, ids, per-particle
@@ -628,6 +756,7 @@ int dispatch(const ffmpm_params& p, Args&&... args) {
     }                                                               \
   };
 FFMPM_OP(SubstepOp, op_substep)
+FFMPM_OP(SubstepHostOp, op_substep_host)
 FFMPM_OP(SortedOp, op_substeps_sorted)
 FFMPM_OP(ProfileOp, op_substeps_sorted)
 FFMPM_OP(P2GOp, op_p2g)
@@ -714,6 +843,25 @@ int ffmpm_substep(const ffmpm_params* p, ffmpm_particles* P, void* ws, size_t ws
   if (P->n == 0) return FFMPM_OK;
   Ws w = bind(ws, L);
   return dispatch<SubstepOp>(*p, L, w, P, static_cast<cudaStream_t>(stream));
+}
+
+int ffmpm_substep_host(const ffmpm_params* p, const ffmpm_particles* host, ffmpm_particles* dev, void* ws,
+                       size_t ws_bytes, void* stream) {
+  Layout L;
+  if (!host || !dev || host->n != dev->n || host->stride != 0 || dev->stride != 0) return FFMPM_ERR_BADARG;
+  int rc = prologue(p, host->n, ws, ws_bytes, &L);
+  if (rc != FFMPM_OK) return rc;
+  if (!particles_ok(*p, host, true) || !particles_ok(*p, dev, true)) return FFMPM_ERR_BADARG;
+  if ((host->mass && !dev->mass) || (host->mu_0 && !dev->mu_0) || (host->lambda_0 && !dev->lambda_0))
+    return FFMPM_ERR_BADARG;
+  if (host->n == 0) return FFMPM_OK;
+  // the device arrays stand in for the host ones: material pointers the host leaves NULL stay NULL
+  ffmpm_particles d = *dev;
+  if (!host->mass) d.mass = nullptr;
+  if (!host->mu_0) d.mu_0 = nullptr;
+  if (!host->lambda_0) d.lambda_0 = nullptr;
+  Ws w = bind(ws, L);
+  return dispatch<SubstepHostOp>(*p, L, w, host, &d, static_cast<cudaStream_t>(stream));
 }
 
 int ffmpm_substeps_sorted(const ffmpm_params* p, ffmpm_particles* a, ffmpm_particles* b, int32_t* ids_a,

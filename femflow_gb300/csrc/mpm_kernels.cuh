@@ -1968,6 +1968,76 @@ __global__ void __launch_bounds__(kThreads) k_g2p(KParams<T> kp, Geom<DIM> g, PV
 }
 
 // ----------------------------------------------------------------------------------------------
+// Substep on particle arrays that live in host memory (ffmpm_substep_host).  The arrays arrive in
+// chunks of particles; each chunk is scattered as soon as it has landed, in the caller's particle
+// order, with one vector atomic per node (a block sort needs every particle, which would hold the
+// scatter back until the last copy).  After a dense grid update each chunk is gathered, again in
+// the caller's order, from the global velocity grid, and copied back while the next chunk is
+// gathered.  Same arithmetic per particle as the sorted kernels (p2g_particle, grid_node,
+// g2p_particle); only the order of the node sums differs.
+
+// P2G of particles [p0, p1): three_d/p2g.py:14-80 / two_d/p2g.py:11-76, straight to the grid.
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kThreads) k_p2g_range(KParams<T> kp, Geom<DIM> g, PView<T> P, uint32_t p0,
+                                                        uint32_t p1, InternalSink<T> sink, int32_t* status,
+                                                        uint32_t* fallbacks) {
+  Geom<DIM> gd = g;
+  gd.tile = g.R + 2;  // origin 0 and a "tile" of the whole grid: every in-grid stencil is accepted
+  DirectAdder<DIM, T, InternalSink<T>> acc;
+  acc.sink = sink;
+  acc.R = g.R;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) acc.org[d] = 0;
+  for (uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += gridDim.x * blockDim.x)
+    p2g_particle<DIM, T>(kp, gd, P, p, acc.org, acc, status, fallbacks);
+}
+
+// Grid update of every node (three_d/grid_op.py:5-47 / two_d/grid_op.py:5-24): momentum of A ->
+// velocity in B, A re-zeroed.  Nodes that received nothing are skipped (their B is never read).
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kThreads) k_grid_update_dense(KParams<T> kp, Geom<DIM> g, Node4<T>* __restrict__ A,
+                                                                Node4<T>* __restrict__ B) {
+  const int R = g.R;
+  const int64_t nn = DIM == 3 ? (int64_t)R * R * R : (int64_t)R * R;
+  for (int64_t node = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; node < nn;
+       node += (int64_t)gridDim.x * blockDim.x) {
+    const Node4<T> a = A[node];
+    if (a.x == T(0) && a.y == T(0) && a.z == T(0) && a.w == T(0)) continue;
+    int I[DIM];
+    if constexpr (DIM == 3) {
+      I[0] = (int)(node / ((int64_t)R * R));
+      I[1] = (int)((node / R) % R);
+      I[2] = (int)(node % R);
+    } else {
+      I[0] = (int)(node / R);
+      I[1] = (int)(node % R);
+    }
+    T vel[3] = {a.x, a.y, a.z};
+    grid_node<DIM, T>(kp, I, vel, a.w);
+    B[node] = Node4<T>{vel[0], vel[1], vel[2], a.w};
+    A[node] = Node4<T>{T(0), T(0), T(0), T(0)};
+  }
+}
+
+// G2P of particles [p0, p1) in place (three_d/g2p.py:9-59 / two_d/g2p.py:5-47), every stencil
+// gathered from the global velocity grid B.
+template <int DIM, typename T>
+__global__ void __launch_bounds__(kThreads) k_g2p_range(KParams<T> kp, Geom<DIM> g, PView<T> P, uint32_t p0,
+                                                        uint32_t p1, const Node4<T>* __restrict__ B, int32_t* status) {
+  G2PExtra ex{};
+  ex.grid_global = B;
+  int org[DIM];
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) org[d] = -(1 << 24);  // no staged tile: every stencil is off-tile
+  const bool need_jp = (DIM == 2) || kp.model == FFMPM_MODEL_SNOW;
+  for (uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += gridDim.x * blockDim.x) {
+    G2PIn<DIM, T> in;
+    g2p_load<DIM, T>(P, p, need_jp, in);
+    g2p_particle<DIM, T>(kp, g, P, P, p, p, org, nullptr, status, false, ex, in);
+  }
+}
+
+// ----------------------------------------------------------------------------------------------
 // Fused G2P + P2G: substep k's G2P and substep k+1's P2G in one pass over the particles.  The
 // updated particle (x, v, C, F) goes straight from the gather into the next substep's record, so
 // v and C never travel through memory between the two, and x and F are read once per substep.

@@ -28,10 +28,18 @@ def solve_mls_mpm_3d(res, inv_dx, hardening, dx, dt, volume, gravity, particles,
 
     ``particles`` is a ``ParticleSet`` (or a list of ``Particle``, converted on the host).  The
     model is fixed to "neo_hookean" as in mls_mpm.py:58.  Host arrays are staged to the GPU and
-    written back.  Raises RuntimeError when a particle leaves the grid.
+    written back; pinned CPU tensors of one dtype take ffmpm_substep_host, whose copies run while
+    its kernels do.  Raises RuntimeError when a particle leaves the grid.
     """
     pset, plist = P.split_particles(particles)
     dtype = P.dtype_of(v, F)
+    host = [pset.pos, pset.mass, pset.mu_0, pset.lambda_0, v, F, C, Jp]
+    if plist is None and P.pinned_host(*host):
+        E._require_cuda()
+        prm = E.make_params(3, res, host[0].dtype, dx, inv_dx, dt, gravity, volume, hardening, model="neo_hookean",
+                            deterministic=deterministic)
+        P.run_host_substep(prm, *host, check=check)
+        return
     st = E.stage([pset.pos, pset.mass, pset.mu_0, pset.lambda_0, v, F, C, Jp], dtype=dtype)
     x, m, mu, lam, vv, FF, CC, JJ = st.dev
     E.check_tensors(dtype, x, m, mu, lam, vv, FF, CC, JJ)

@@ -160,6 +160,22 @@ int ffmpm_g2p(const ffmpm_params *p, const ffmpm_grid *grid, ffmpm_particles *P,
  * arrays, in place, particle order preserved.  The grid lives in the workspace. */
 int ffmpm_substep(const ffmpm_params *p, ffmpm_particles *P, void *ws, size_t ws_bytes, void *stream);
 
+/* solve_mls_mpm_3d (mls_mpm.py:40-79) and its 2D analogue on particle arrays in HOST memory
+ * (`host`: the row-major layouts above, stride 0; pinned memory lets the copies run while the
+ * kernels do).  The arrays go to the caller's device arrays `dev` (same shapes; mass / mu_0 /
+ * lambda_0 only where the host gives them), the substep runs there, and x, v, F, C, Jp come back
+ * into the host arrays.  Uploads and the scatter, and the gather and the downloads, are pipelined
+ * over chunks of particles: each chunk is scattered in the caller's order as soon as it has landed
+ * (one vector atomic per node, no block sort), the grid update covers every node, and each chunk
+ * is gathered and sent back while the next one is gathered.  Same arithmetic per particle as
+ * ffmpm_substep; the node sums run in another order.  The deterministic mode uploads everything,
+ * runs ffmpm_substep and downloads.  The copies use two streams and a few events of the library's
+ * own, created by the first call on a device and kept until exit: make that first call before any
+ * stream capture.  Everything is ordered after the work already queued on `stream`, and the host
+ * arrays hold the result once `stream` has run. */
+int ffmpm_substep_host(const ffmpm_params *p, const ffmpm_particles *host, ffmpm_particles *dev, void *ws,
+                       size_t ws_bytes, void *stream);
+
 /* `nsteps` substeps that keep the particles physically sorted by grid block: step k reads
  * buffer (k even ? a : b) and writes the other one in sorted order, carrying the particle ids
  * (ids_a/ids_b) along.  After the call the state is in `a` when nsteps is even, else in `b`.
