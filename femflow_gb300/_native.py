@@ -102,6 +102,8 @@ _PROTOS = {
     "ffmpm_substep_host": (ctypes.c_int, [_P(Params), _P(Particles), _P(Particles), _vp, ctypes.c_size_t, _vp]),
     "ffmpm_substeps_sorted": (ctypes.c_int, [_P(Params), _P(Particles), _P(Particles), _vp, _vp, ctypes.c_int32,
                                              _vp, ctypes.c_size_t, _vp]),
+    "ffmpm_substeps_sorted_snapshots": (ctypes.c_int, [_P(Params), _P(Particles), _P(Particles), _vp, _vp,
+                                                       ctypes.c_int32, _vp, _vp, _vp, ctypes.c_size_t, _vp]),
     "ffmpm_sort_by_block": (ctypes.c_int, [_P(Params), _vp, ctypes.c_int64, _vp, _vp, _vp, ctypes.c_size_t, _vp]),
     "ffmpm_diagnostics_fp64": (ctypes.c_int, [_P(Params), _P(Particles), _vp, _vp]),
     "ffmpm_profile_substeps": (ctypes.c_int, [_P(Params), _P(Particles), _P(Particles), _vp, _vp, ctypes.c_int32,

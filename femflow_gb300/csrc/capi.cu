@@ -582,6 +582,27 @@ int op_substep_host(const ffmpm_params& p, const Layout& L, const Ws& w, const f
   return check_launch();
 }
 
+// Per-substep copies of the positions and ids (ffmpm_substeps_sorted_snapshots): after substep k
+// the output buffer's x (dim components of n reals, in its sorted order) goes to x + k dim n and
+// its ids to ids + k n, on the run's stream.
+struct SnapOut {
+  void* x;
+  int32_t* ids;
+};
+
+template <int DIM, typename T>
+void snapshot(const SnapOut* snap, int k, const PView<T>& out, const int32_t* ids_out, int64_t n, cudaStream_t s) {
+  if (!snap) return;
+  T* dst = static_cast<T*>(snap->x) + (size_t)k * DIM * n;
+  if (out.soa == n) {
+    cudaMemcpyAsync(dst, out.x, sizeof(T) * DIM * n, cudaMemcpyDeviceToDevice, s);
+  } else {
+    for (int d = 0; d < DIM; ++d)
+      cudaMemcpyAsync(dst + (size_t)d * n, out.x + (size_t)d * out.soa, sizeof(T) * n, cudaMemcpyDeviceToDevice, s);
+  }
+  cudaMemcpyAsync(snap->ids + (size_t)k * n, ids_out, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, s);
+}
+
 // Substeps 0..n-1 with the fused kernel: P2G(0), then for k = 0..n-2: grid update(k), re-sort if
 // due (k a multiple of the cadence), G2P(k) + P2G(k+1); then grid update(n-1) and G2P(n-1).  The
 // state after every substep is in buffer a or b as in the unfused loop (x, F, Jp, ids, per-particle
@@ -593,7 +614,7 @@ int op_substep_host(const ffmpm_params& p, const Layout& L, const Ws& w, const f
 // that precedes a re-sort.
 template <int DIM, typename T>
 int op_substeps_fused(const ffmpm_params& p, const Layout& L, const Ws& w, PView<T> va, PView<T> vb, int32_t* ids_a,
-                      int32_t* ids_b, int nsteps, cudaStream_t s, PhaseTimer* tm) {
+                      int32_t* ids_b, int nsteps, cudaStream_t s, PhaseTimer* tm, const SnapOut* snap) {
   const int K = sort_every(p);
   const auto resorts = [&](int k) { return k >= 1 && k <= nsteps - 2 && k % K == 0; };
   const uint32_t* sorted_perm = nullptr;
@@ -617,6 +638,7 @@ int op_substeps_fused(const ffmpm_params& p, const Layout& L, const Ws& w, PView
       const int rc = launch_g2p<DIM, T, true, true>(p, L, w, in, out, nullptr, nullptr, ex, s);
       if (tm) tm->end(1);
       if (rc != FFMPM_OK) return rc;
+      snapshot<DIM, T>(snap, k, out, ids_out, L.n, s);
       break;
     }
     if (k > 0) perm = nullptr;
@@ -628,15 +650,17 @@ int op_substeps_fused(const ffmpm_params& p, const Layout& L, const Ws& w, PView
     const int rc = launch_g2p2g<DIM, T>(p, L, w, in, out, perm, ex, s, nullptr);
     if (tm) tm->end(1);
     if (rc != FFMPM_OK) return rc;
+    snapshot<DIM, T>(snap, k, out, ids_out, L.n, s);
   }
   return check_launch();
 }
 
 template <int DIM, typename T>
 int op_substeps_sorted(const ffmpm_params& p, const Layout& L, const Ws& w, ffmpm_particles* a, ffmpm_particles* b,
-                       int32_t* ids_a, int32_t* ids_b, int nsteps, cudaStream_t s, PhaseTimer* tm = nullptr) {
+                       int32_t* ids_a, int32_t* ids_b, int nsteps, cudaStream_t s, PhaseTimer* tm = nullptr,
+                       const SnapOut* snap = nullptr) {
   PView<T> va = pview<T>(*a), vb = pview<T>(*b);
-  if (fused(p, L, nsteps)) return op_substeps_fused<DIM, T>(p, L, w, va, vb, ids_a, ids_b, nsteps, s, tm);
+  if (fused(p, L, nsteps)) return op_substeps_fused<DIM, T>(p, L, w, va, vb, ids_a, ids_b, nsteps, s, tm, snap);
   const int K = sort_every(p);
   const uint32_t* flag = K > 1 ? &w.hdr->sort_now : nullptr;
   for (int k = 0; k < nsteps; ++k) {
@@ -665,6 +689,7 @@ int op_substeps_sorted(const ffmpm_params& p, const Layout& L, const Ws& w, ffmp
     int rc = launch_g2p<DIM, T, true, true>(p, L, w, in, out, perm, nullptr, ex, s, flag);
     if (tm) tm->end(1);
     if (rc != FFMPM_OK) return rc;
+    snapshot<DIM, T>(snap, k, out, ids_out, L.n, s);
   }
   // The last G2P counted the blocks of the final state for a substep that will not run here:
   // clear the histogram so the workspace invariant (zero between calls) holds.
@@ -759,6 +784,7 @@ FFMPM_OP(SubstepOp, op_substep)
 FFMPM_OP(SubstepHostOp, op_substep_host)
 FFMPM_OP(SortedOp, op_substeps_sorted)
 FFMPM_OP(ProfileOp, op_substeps_sorted)
+FFMPM_OP(SnapshotOp, op_substeps_sorted)
 FFMPM_OP(P2GOp, op_p2g)
 FFMPM_OP(G2POp, op_g2p)
 FFMPM_OP(GridOp, op_grid_op)
@@ -877,6 +903,25 @@ int ffmpm_substeps_sorted(const ffmpm_params* p, ffmpm_particles* a, ffmpm_parti
   if (a->n == 0 || nsteps == 0) return FFMPM_OK;
   Ws w = bind(ws, L);
   return dispatch<SortedOp>(*p, L, w, a, b, ids_a, ids_b, (int)nsteps, static_cast<cudaStream_t>(stream));
+}
+
+int ffmpm_substeps_sorted_snapshots(const ffmpm_params* p, ffmpm_particles* a, ffmpm_particles* b, int32_t* ids_a,
+                                    int32_t* ids_b, int32_t nsteps, void* snap_x, int32_t* snap_ids, void* ws,
+                                    size_t ws_bytes, void* stream) {
+  Layout L;
+  if (!a || !b || nsteps < 0 || a->n != b->n || !ids_a || !ids_b || !snap_x || !snap_ids) return FFMPM_ERR_BADARG;
+  if (a->stride < a->n || b->stride < b->n) return FFMPM_ERR_BADARG;  // component-major buffers only
+  int rc = prologue(p, a->n, ws, ws_bytes, &L);
+  if (rc != FFMPM_OK) return rc;
+  if (!particles_ok(*p, a, true) || !particles_ok(*p, b, true)) return FFMPM_ERR_BADARG;
+  if ((a->mass != nullptr) != (b->mass != nullptr) || (a->mu_0 != nullptr) != (b->mu_0 != nullptr) ||
+      (a->lambda_0 != nullptr) != (b->lambda_0 != nullptr))
+    return FFMPM_ERR_BADARG;
+  if (a->n == 0 || nsteps == 0) return FFMPM_OK;
+  Ws w = bind(ws, L);
+  const SnapOut snap{snap_x, snap_ids};
+  return dispatch<SnapshotOp>(*p, L, w, a, b, ids_a, ids_b, (int)nsteps, static_cast<cudaStream_t>(stream),
+                              static_cast<PhaseTimer*>(nullptr), &snap);
 }
 
 int ffmpm_profile_substeps(const ffmpm_params* p, ffmpm_particles* a, ffmpm_particles* b, int32_t* ids_a,

@@ -98,42 +98,55 @@ class MPMSolver:
         self._graph_steps = 0
 
     # ------------------------------------------------------------------ stepping
-    def _launch(self, nsteps: int):
+    def _call(self, nsteps: int, stream_ptr: int, snapshots=None):
         sa, sb = self._cur.struct(), self._oth.struct()
-        N.call("ffmpm_substeps_sorted", ctypes.byref(self.params), ctypes.byref(sa), ctypes.byref(sb),
-               ctypes.c_void_p(self._cur.ids.data_ptr()), ctypes.c_void_p(self._oth.ids.data_ptr()),
-               int(nsteps), ctypes.c_void_p(self.ws.ptr), ctypes.c_size_t(self.ws.bytes),
-               ctypes.c_void_p(E._stream_ptr(self.device)))
+        head = (ctypes.byref(self.params), ctypes.byref(sa), ctypes.byref(sb),
+                ctypes.c_void_p(self._cur.ids.data_ptr()), ctypes.c_void_p(self._oth.ids.data_ptr()), int(nsteps))
+        tail = (ctypes.c_void_p(self.ws.ptr), ctypes.c_size_t(self.ws.bytes), ctypes.c_void_p(stream_ptr))
+        if snapshots is None:
+            N.call("ffmpm_substeps_sorted", *head, *tail)
+        else:
+            sx, si = snapshots
+            if sx.shape[0] < nsteps or si.shape[0] < nsteps or sx.dtype != self.dtype or si.dtype != torch.int32:
+                raise ValueError("snapshot arrays: x [>= nsteps, dim, n] of the solver's dtype, ids [>= nsteps, n] int32")
+            N.call("ffmpm_substeps_sorted_snapshots", *head, ctypes.c_void_p(sx.data_ptr()),
+                   ctypes.c_void_p(si.data_ptr()), *tail)
+
+    def _launch(self, nsteps: int, snapshots=None):
+        self._call(nsteps, E._stream_ptr(self.device), snapshots)
         if nsteps % 2 == 1:
             self._cur, self._oth = self._oth, self._cur
         self.steps_done += nsteps
 
-    def step(self, nsteps: int = 1, check: bool = False):
-        """Run ``nsteps`` substeps (stream-ordered, asynchronous unless ``check``)."""
-        if self._graph is not None and nsteps % self._graph_steps == 0:
+    def step(self, nsteps: int = 1, check: bool = False, snapshots=None):
+        """Run ``nsteps`` substeps (stream-ordered, asynchronous unless ``check``).  ``snapshots``:
+        device arrays (x [>= nsteps, dim, n] of the solver's dtype, ids [>= nsteps, n] int32) that
+        receive every substep's positions in block-sorted order and the ids that go with them (the
+        positions of particle ids[k][i] are x[k][:, i]); a captured graph replays with the arrays
+        it was captured with."""
+        if self._graph is not None and nsteps % self._graph_steps == 0 and snapshots is None:
             for _ in range(nsteps // self._graph_steps):
                 self._graph.replay()
             self.steps_done += nsteps
         else:
-            self._launch(nsteps)
+            self._launch(nsteps, snapshots)
         if check:
             self.ws.raise_on_status()
 
-    def capture(self, nsteps: int):
-        """Capture ``nsteps`` (even) substeps into a CUDA graph; ``step`` then replays it."""
+    def capture(self, nsteps: int, snapshots=None, warmup: bool = True):
+        """Capture ``nsteps`` (even) substeps into a CUDA graph; ``step`` then replays it (with the
+        ``snapshots`` arrays, when given).  ``warmup`` first runs two substeps directly, so that the
+        first-call set-up happens outside the capture; pass False when the solver has run before."""
         if nsteps <= 0 or nsteps % 2:
             raise ValueError("graph capture needs an even number of substeps (state returns to its buffer)")
-        self._launch(2)  # warm up (first-call set-up happens outside the capture)
+        if warmup:
+            self._launch(2)
         torch.cuda.synchronize(self.device)
         g = torch.cuda.CUDAGraph()
         s = torch.cuda.Stream(self.device)
         with torch.cuda.stream(s):
             with torch.cuda.graph(g, stream=s):
-                sa, sb = self._cur.struct(), self._oth.struct()
-                N.call("ffmpm_substeps_sorted", ctypes.byref(self.params), ctypes.byref(sa), ctypes.byref(sb),
-                       ctypes.c_void_p(self._cur.ids.data_ptr()), ctypes.c_void_p(self._oth.ids.data_ptr()),
-                       int(nsteps), ctypes.c_void_p(self.ws.ptr), ctypes.c_size_t(self.ws.bytes),
-                       ctypes.c_void_p(s.cuda_stream))
+                self._call(nsteps, s.cuda_stream, snapshots)
         torch.cuda.synchronize(self.device)
         self._graph, self._graph_steps = g, nsteps
         return g

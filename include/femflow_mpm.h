@@ -183,6 +183,16 @@ int ffmpm_substep_host(const ffmpm_params *p, const ffmpm_particles *host, ffmpm
 int ffmpm_substeps_sorted(const ffmpm_params *p, ffmpm_particles *a, ffmpm_particles *b, int32_t *ids_a,
                           int32_t *ids_b, int32_t nsteps, void *ws, size_t ws_bytes, void *stream);
 
+/* ffmpm_substeps_sorted that also keeps every substep's positions, for a caller that hands each
+ * substep's positions out while the run goes on (MPMSimulation._simulate_offline appends them
+ * after every substep, simulation.py:140-142).  a and b must be component-major (stride >= n)
+ * and carry ids.  After substep k the positions of the buffer the substep wrote (dim components of
+ * n reals, in its block-sorted order) are copied to snap_x + k * dim * n and its ids to
+ * snap_ids + k * n (device arrays, real type of p): particle snap_ids[k][i] sits at column i. */
+int ffmpm_substeps_sorted_snapshots(const ffmpm_params *p, ffmpm_particles *a, ffmpm_particles *b, int32_t *ids_a,
+                                    int32_t *ids_b, int32_t nsteps, void *snap_x, int32_t *snap_ids, void *ws,
+                                    size_t ws_bytes, void *stream);
+
 /* Stable radix sort of the particles by grid-block key (the block of each particle's base node,
  * then its cell inside the block): keys_out[i] is the i-th smallest key, perm_out[i] the index of
  * that particle.  Particles outside the grid get key 0xFFFFFFFF and sort last.  No reference
