@@ -128,6 +128,9 @@ _PROTOS = {
     "ffmpm_mlp_train_backward": (ctypes.c_int, [_P(MLPTrainer), _vp, _vp, ctypes.c_int32, _vp, _vp]),
     "ffmpm_mlp_train_update": (ctypes.c_int, [_P(MLPTrainer), ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                               ctypes.c_float, ctypes.c_int32, _vp]),
+    "ffmpm_implicit_points_workspace_size": (ctypes.c_int, [ctypes.c_int32, _P(ctypes.c_size_t)]),
+    "ffmpm_implicit_points": (ctypes.c_int, [ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32, _vp,
+                                             ctypes.c_int64, _vp, _vp, ctypes.c_size_t, _vp]),
     "ffmpm_version": (ctypes.c_char_p, []),
 }
 

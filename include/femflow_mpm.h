@@ -253,6 +253,27 @@ int ffmpm_kernels_per_call(const ffmpm_params *p, int64_t n, int32_t nsteps, int
 int ffmpm_sort_by_block_static(const ffmpm_params *p, const void *x, int64_t n, uint32_t *keys_out,
                                uint32_t *perm_out, int32_t *status_out, void *stream);
 
+/* ---- scene sampling ---- */
+
+/* The reference's triply periodic surfaces (femflow/simulation/mpm/primitives.py:9-38). */
+#define FFMPM_TPMS_GYROID 0
+#define FFMPM_TPMS_DIAMOND 1
+#define FFMPM_TPMS_PRIMITIVE 2
+#define FFMPM_IMPLICIT_MAX_RES 1024
+
+/* Workspace bytes of ffmpm_implicit_points for a res^3 lattice (16-byte aligned workspace). */
+int ffmpm_implicit_points_workspace_size(int32_t res, size_t *bytes);
+
+/* generate_implicit_points(kind, k, t, res) (primitives.py:46-61): the points of the res^3 lattice
+ * in [0, 1]^3 (numerics/geometry.py:100-116, first axis fastest, coordinate i / (res - 1)) whose
+ * implicit value (which has t subtracted already) is larger than t, in lattice order, written to
+ * points[count][3] (device, float64).  *count (device int64) receives the number of such points
+ * even when it exceeds `capacity`; points beyond capacity are not written (call with capacity 0
+ * to size the output).  float64 arithmetic with each product and sum rounded on its own, in the
+ * reference's order.  1 <= res <= FFMPM_IMPLICIT_MAX_RES, k finite and nonzero. */
+int ffmpm_implicit_points(int32_t kind, double k, double t, int32_t res, double *points, int64_t capacity,
+                          int64_t *count, void *ws, size_t ws_bytes, void *stream);
+
 /* ---- batched 2D scenes: one persistent launch per substep for many independent scenes ---- */
 #define FFMPM_BATCH2D_MAX_SCENES 256
 

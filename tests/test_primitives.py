@@ -11,11 +11,15 @@ def test_grid_matches_reference():
     np.testing.assert_array_equal(P.grid((5, 1, 3)), d["grid_5_1_3"])
 
 
-def test_implicit_points_match_reference():
+def test_implicit_points_of_a_callers_own_function_match_reference():
+    """A caller's own implicit function is called point by point, as the reference calls it (the
+    reference's three surfaces go to the GPU; tests/test_gpu_primitives.py)."""
     d = load("primitives")
     for fn in ("gyroid", "diamond", "primitive"):
-        np.testing.assert_allclose(P.generate_implicit_points(fn, 0.35, 0.15, 12), d[f"{fn}_a"], rtol=0, atol=0)
-        np.testing.assert_allclose(P.generate_implicit_points(fn, 0.5, -0.3, 9), d[f"{fn}_b"], rtol=0, atol=0)
+        f = getattr(P, fn)
+        own = lambda k, t, pos, f=f: f(k, t, pos)
+        np.testing.assert_allclose(P.generate_implicit_points(own, 0.35, 0.15, 12), d[f"{fn}_a"], rtol=0, atol=0)
+        np.testing.assert_allclose(P.generate_implicit_points(own, 0.5, -0.3, 9), d[f"{fn}_b"], rtol=0, atol=0)
 
 
 def test_cube_points_match_reference():
