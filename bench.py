@@ -217,6 +217,28 @@ def run_ours(args):
                                  "steps": e_steps, "sort_every": 1, "cuda_graph_substeps": 40}
     del every
 
+    # ---- batched 2D scenes: 256 seeded scenes (2k-64k particles, grids 64^2-256^2, E capped at
+    # elastic CFL 0.5 per scene), autotuned launch shape, one 100-substep CUDA graph
+    from femflow_gb300.batched import Batch2D, random_scenes, stable_variant
+
+    bt = Batch2D(stable_variant(random_scenes(256, seed=0)), dtype=torch.float32, device=dev)
+    shape, _ = bt.autotune(steps=1)
+    bt.capture(100)
+    bt.step(100)
+    torch.cuda.synchronize(dev)
+    b_steps = 300
+    barrier()
+    ev0.record(stream)
+    bt.step(b_steps)
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    tb = REP.max_over_ranks(ev0.elapsed_time(ev1) / 1e3, dev)
+    out["batched_2d_256_scenes"] = {"value": world * bt.n * b_steps / tb, "unit": UNIT, "ms_per_step": 1e3 * tb / b_steps,
+                                    "scenes": 256, "particles": bt.n, "steps": b_steps, "cuda_graph_substeps": 100,
+                                    "launch_shape": {"threads": shape[0], "ctas_per_sm": shape[1]},
+                                    "status": bt.status()}
+    del bt
+
     # ---- per-kernel times (CUDA events around each phase, same stream) for the roofline
     pro_steps = min(args.steps, 40)
     prof = solver.profile(pro_steps)

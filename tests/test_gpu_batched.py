@@ -76,3 +76,31 @@ def test_batch_graph_replay_and_autotune():
     c.step(9)
     close(n(a2.scene_state(2)["x"]), n(c.scene_state(2)["x"]), 1e-12, scale=1.0, what="graph vs direct")
     assert a.status() == 0 and a2.status() == 0
+
+
+def test_batch_256_scenes_graph_against_oracle():
+    """The batched workload at full scale: 256 seeded scenes (2k-64k particles each, grids 64^2 to
+    256^2, the stable variant of E), autotuned launch shape, one 100-substep CUDA graph; a seeded
+    sample of scenes against the oracle's 2D substep after the 100 substeps."""
+    from femflow_gb300.batched import stable_variant
+
+    sc = stable_variant(random_scenes(256, seed=0))
+    b = Batch2D(sc, dtype=torch.float32)
+    b.autotune(steps=1)  # advances every scene by the substeps used for timing
+    b.reset()  # zero the grids and the status; the particle state keeps the autotuning substeps
+    start = [b.scene_state(i) for i in range(len(sc))]
+    b.capture(100)  # one direct substep before the capture
+    b.step(100)
+    assert b.status() == 0
+    rng = np.random.default_rng(7)
+    sample = sorted(rng.choice(len(sc), size=5, replace=False, p=None))
+    for i in sample:
+        s, st0 = sc[i], start[i]
+        x, v = n(st0["x"]), n(st0["v"])
+        F, C, Jp = n(st0["F"]), n(st0["C"]), n(st0["Jp"]).reshape(-1, 1)
+        for _ in range(101):
+            O.substep_2d(s["res"], float(s["res"]), 1.0, s["mu_0"], s["lambda_0"], s["mass"], 1.0 / s["res"], s["dt"],
+                         s["volume"], -9.8, x, v, F, C, Jp)
+        got = b.scene_state(i)
+        close(n(got["x"]), x, 1e-5, scale=1.0, what=f"scene {i} x")
+        close(n(got["v"]), v, 1e-3, scale=max(np.abs(v).max(), 1e-3), what=f"scene {i} v")
