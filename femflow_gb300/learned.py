@@ -267,8 +267,20 @@ def make_targets(st: Stepper, coarse_buf: torch.Tensor, fine_buf: torch.Tensor) 
     return torch.cat([dF, dv], dim=1).contiguous()
 
 
-def generate(specs, res=128, dt=5e-5, ratio=8, samples_per_scene=5, warm=40, gap=16, device="cuda"):
-    """Features (bf16 [S][128], unscaled) and targets (float32 [S][12]) from fine rollouts."""
+def _keep_rows(X, T, keep: float, gen: torch.Generator):
+    """A random fraction `keep` of the rows of one sample (all rows for keep >= 1)."""
+    if keep >= 1.0:
+        return X, T
+    m = max(1, int(X.shape[0] * keep))
+    idx = torch.randperm(X.shape[0], generator=gen, device="cpu")[:m].to(X.device)
+    return X[idx], T[idx]
+
+
+def generate(specs, res=128, dt=5e-5, ratio=8, samples_per_scene=5, warm=40, gap=16, device="cuda", keep=1.0):
+    """Features (bf16 [S][128], unscaled) and targets (float32 [S][12]) from fine rollouts; `keep`
+    keeps a random fraction of each sample's particles (scenes as dense as the evaluated one without
+    the full data volume)."""
+    gen = torch.Generator().manual_seed(1234)
     feats, targs = [], []
     for spec in specs:
         st = Stepper(spec, res, dt, ratio, device=device)
@@ -281,12 +293,55 @@ def generate(specs, res=128, dt=5e-5, ratio=8, samples_per_scene=5, warm=40, gap
             st.coarse_step(tmp, None, X)
             for _ in range(ratio):
                 st.fine_step(buf)
-            feats.append(X)
-            targs.append(make_targets(st, tmp, buf))
+            Xk, Tk = _keep_rows(X, make_targets(st, tmp, buf), keep, gen)
+            feats.append(Xk)
+            targs.append(Tk)
             for _ in range(gap):
                 st.fine_step(buf)
         st.check()
     return torch.cat(feats), torch.cat(targs)
+
+
+def generate_on_policy(specs, cor_for, res=128, dt=5e-5, ratio=8, samples_per_scene=5, warm=5, gap=2,
+                       device="cuda", keep=1.0):
+    """Features and targets on the trajectory of the corrected coarse step itself: the state
+    advances by corrected coarse steps (``cor_for(stepper)`` gives the Corrector), and at each sample
+    point the target is the fine rollout of ``ratio`` substeps from that state against a plain coarse
+    step from it.  Training on these states teaches the network the states it meets when it runs in
+    closed loop, which fine rollouts alone do not show it.  A scene whose corrected trajectory
+    leaves the grid contributes nothing (its status is cleared); the number of such scenes is
+    returned third."""
+    feats, targs, dropped = [], [], 0
+    gen = torch.Generator().manual_seed(4321)
+    for spec in specs:
+        st = Stepper(spec, res, dt, ratio, device=device)
+        cor = cor_for(st)
+        buf = st.initial_state()
+        f_scene, t_scene = [], []
+        for _ in range(warm):
+            st.coarse_step(buf, cor)
+        for _ in range(samples_per_scene):
+            tmp = buf.clone()
+            X = torch.empty((st.n, N.MLP_IN), dtype=torch.bfloat16, device=st.device)
+            st.coarse_step(tmp, None, X)
+            fine = buf.clone()
+            for _ in range(ratio):
+                st.fine_step(fine)
+            Xk, Tk = _keep_rows(X, make_targets(st, tmp, fine), keep, gen)
+            f_scene.append(Xk)
+            t_scene.append(Tk)
+            for _ in range(1 + gap):
+                st.coarse_step(buf, cor)
+        if st.ws.status()[0] != 0 or int(st.status.item()) != 0:
+            st.ws.clear_status()
+            st.status.zero_()
+            dropped += 1
+            continue
+        feats += f_scene
+        targs += t_scene
+    if not feats:
+        return None, None, dropped
+    return torch.cat(feats), torch.cat(targs), dropped
 
 
 def training_specs(n_scenes: int, n_per_cube: int, seed: int = 0, E_range=(50.0, 200.0)):

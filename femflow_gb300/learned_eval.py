@@ -5,7 +5,11 @@
 1. Data: fine-dt rollouts of ``--scenes`` seeded two-cube scenes (E log-uniform in --E-range, nu in
    [0.2, 0.35], speeds in [0.5, 1.5], textbook fixed-corotated stress), ``--samples`` sample points
    each (one coarse step exported, k fine steps as the target).
-2. Training on the tensor cores (``learned.train``).
+2. Training on the tensor cores (``learned.train``), then ``onpolicy_rounds`` rounds that add samples
+   taken on the trajectory of the velocity-corrected coarse step itself (``generate_on_policy``)
+   and train on the union.  A network trained on fine-rollout states alone makes the closed-loop
+   error worse (its corrections move the state to where it has seen no data); the on-policy
+   samples teach it the states it meets when it runs.
 3. Selection on a held-out validation scene (its own seed) at the evaluation horizon: the corrected
    outputs ("v": velocity only, "all": velocity and F) and the strength in {0, 1/4, 1/2, 1}; strength
    0 (the network off) is always a candidate, so the selected form is never worse than the plain
@@ -45,9 +49,22 @@ def select(net: L.Net, spec: L.SceneSpec, res, dt, ratio, horizon) -> dict:
             for _ in range(horizon):
                 st.coarse_step(b, cor)
             err = L.position_error(b, fine)["max"]
-            trials.append(dict(mode=mode, strength=a, err_max=err if err == err else float("inf")))
+            # a trial whose corrections drove a particle out of the grid fails (and must not leave
+            # its status bits to the next one)
+            left_grid = st.ws.status()[0] != 0 or int(st.status.item()) != 0
+            if left_grid:
+                st.ws.clear_status()
+                st.status.zero_()
+            ok = err == err and not left_grid
+            trials.append(dict(mode=mode, strength=a, err_max=err if ok else float("inf")))
     best = min(trials, key=lambda t: t["err_max"])
     return dict(best=best, trials=trials)
+
+
+def velocity_corrector(net, st, strength):
+    cor = L.Corrector(net, st, strength)
+    cor.out_scale[0:9] = 0.0
+    return cor
 
 
 def corrector_for(net, st, choice):
@@ -57,31 +74,55 @@ def corrector_for(net, st, choice):
     return cor
 
 
-def run(res=128, dt=5e-5, ratio=8, scenes=64, per_cube=16384, samples=4, steps=4000, batch=32768, horizon=50,
-        n_per_cube=524288, E_eval=120.0, E_range=(50.0, 200.0), seed=0) -> dict:
+def run(res=128, dt=5e-5, ratio=8, scenes=16, per_cube=524288, samples=4, steps=4000, batch=32768, horizon=150,
+        n_per_cube=524288, E_eval=120.0, E_range=(50.0, 200.0), seed=0, onpolicy_rounds=3, onpolicy_samples=8,
+        onpolicy_gap=10, round_steps=None, keep=1.0 / 16) -> dict:
     rep = dict(res=res, dt_fine=dt, ratio=ratio, dt_coarse=dt * ratio, horizon_coarse_steps=horizon,
                simulated_time=horizon * ratio * dt, E_range=E_range, E_eval=E_eval, model="fixed_corotated")
     t0 = time.perf_counter()
     specs = L.training_specs(scenes, per_cube, seed=seed, E_range=E_range)
-    X, T = L.generate(specs, res=res, dt=dt, ratio=ratio, samples_per_scene=samples, warm=20, gap=24)
+    X, T = L.generate(specs, res=res, dt=dt, ratio=ratio, samples_per_scene=samples, warm=20, gap=40, keep=keep)
     torch.cuda.synchronize()
-    rep["samples"] = int(X.shape[0])
+    rep["samples_fine_rollouts"] = int(X.shape[0])
     rep["data_seconds"] = time.perf_counter() - t0
     net = L.Net(max_batch=batch, seed=seed)
     L.fit_scales(net, X, T)
     Xs, Ts = L.scaled(net, X, T)
-    del X, T
     nval = min(Xs.shape[0] // 10 // batch * batch, 8 * batch)
-    base = L.evaluate_loss(net, Xs[-nval:], Ts[-nval:], batch)
+    Xv, Tv = Xs[-nval:].clone(), Ts[-nval:].clone()
+    base = L.evaluate_loss(net, Xv, Tv, batch)
     t0 = time.perf_counter()
     log = L.train(net, Xs[:-nval], Ts[:-nval], steps=steps, batch=batch, lr=2e-3, seed=seed)
+    del Xs, Ts
+    rep["val_loss_untrained"] = base
+    rep["val_loss_trained"] = L.evaluate_loss(net, Xv, Tv, batch)
+    # on-policy rounds: samples on the velocity-corrected coarse trajectory, training on the union
+    round_steps = round_steps or max(1, (3 * steps) // 4)
+    rep["onpolicy"] = []
+    for rnd in range(onpolicy_rounds):
+        t1 = time.perf_counter()
+        # the collecting correction grows over the rounds (0.25, 0.5, 1): a network trained on
+        # fine-rollout states alone can drive every scene out of the grid at full strength
+        a = min(1.0, 0.25 * 2 ** rnd)
+        Xo, To, dropped = L.generate_on_policy(specs, lambda st: velocity_corrector(net, st, a), res=res, dt=dt,
+                                               ratio=ratio, samples_per_scene=onpolicy_samples, warm=5,
+                                               gap=onpolicy_gap, keep=keep)
+        if Xo is None:  # every scene left the grid: no samples this round
+            rep["onpolicy"].append(dict(round=rnd + 1, strength=a, samples=int(X.shape[0]), scenes_left_grid=dropped))
+            continue
+        X, T = torch.cat([X, Xo]), torch.cat([T, To])
+        del Xo, To
+        Xs, Ts = L.scaled(net, X, T)
+        log += L.train(net, Xs, Ts, steps=round_steps, batch=batch, lr=2e-3, seed=seed + 1 + rnd)
+        del Xs, Ts
+        torch.cuda.synchronize()
+        rep["onpolicy"].append(dict(round=rnd + 1, strength=a, samples=int(X.shape[0]), scenes_left_grid=dropped,
+                                    seconds=time.perf_counter() - t1))
+    del X, T
     torch.cuda.synchronize()
     rep["train_seconds"] = time.perf_counter() - t0
-    rep["train_steps"], rep["batch"] = steps, batch
+    rep["train_steps"], rep["batch"] = steps + onpolicy_rounds * round_steps, batch
     rep["train_loss_log"] = log[:: max(1, len(log) // 10)]
-    rep["val_loss_untrained"] = base
-    rep["val_loss_trained"] = L.evaluate_loss(net, Xs[-nval:], Ts[-nval:], batch)
-    del Xs, Ts
     val_spec = L.SceneSpec(n_per_cube=per_cube * 2, E=E_eval, nu=0.3, speed=1.0, seed=seed * 1000 + 777)
     sel = select(net, val_spec, res, dt, ratio, horizon)
     rep["selection"] = sel
@@ -150,18 +191,20 @@ def main(argv=None):
     ap.add_argument("--res", type=int, default=128)
     ap.add_argument("--dt", type=float, default=5e-5)
     ap.add_argument("--ratio", type=int, default=8)
-    ap.add_argument("--scenes", type=int, default=64)
-    ap.add_argument("--per-cube", type=int, default=16384)
+    ap.add_argument("--scenes", type=int, default=16)
+    ap.add_argument("--per-cube", type=int, default=524288)
+    ap.add_argument("--keep", type=float, default=1.0 / 16, help="fraction of each sample's particles kept")
     ap.add_argument("--samples", type=int, default=4)
     ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--batch", type=int, default=32768)
-    ap.add_argument("--horizon", type=int, default=50)
+    ap.add_argument("--horizon", type=int, default=150)
+    ap.add_argument("--onpolicy-rounds", type=int, default=3)
     ap.add_argument("--n-per-cube", type=int, default=524288)
     ap.add_argument("--E", type=float, default=120.0)
     ap.add_argument("--seed", type=int, default=0)
     a = ap.parse_args(argv)
     r = run(a.res, a.dt, a.ratio, a.scenes, a.per_cube, a.samples, a.steps, a.batch, a.horizon, a.n_per_cube, a.E,
-            seed=a.seed)
+            seed=a.seed, onpolicy_rounds=a.onpolicy_rounds, keep=a.keep)
     print(json.dumps(r, indent=1, default=float))
 
 

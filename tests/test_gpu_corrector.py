@@ -137,17 +137,24 @@ def test_fused_corrector_matches_unfused_forward():
 
 
 def test_learned_corrector_small_end_to_end():
-    """Data from fine rollouts, tensor-core training, selection on a held-out scene and the timed
-    comparison with the plain fine and plain coarse rollouts (small: 2 x 32,768 particles, 64^3)."""
+    """Data from fine rollouts and from the corrected coarse trajectory (on-policy rounds),
+    tensor-core training, selection on a held-out scene, and the timed comparison with the plain
+    fine and plain coarse rollouts over a horizon that includes the two cubes' collision (small:
+    2 x 32,768 particles, 64^3, 100 coarse steps of 8 x 1e-4).  The trained network must reduce the
+    coarse step's error against the fine rollout."""
     from femflow_gb300 import learned_eval as LE
-    r = LE.run(res=64, dt=1e-4, ratio=8, scenes=16, per_cube=8192, samples=4, steps=800, batch=16384, horizon=25,
-               n_per_cube=32768, E_eval=120.0)
+    r = LE.run(res=64, dt=1e-4, ratio=8, scenes=24, per_cube=8192, samples=6, steps=800, batch=16384, horizon=100,
+               n_per_cube=32768, E_eval=120.0, onpolicy_rounds=3, round_steps=600, keep=1.0)
     assert r["val_loss_trained"] < 0.8 * r["val_loss_untrained"], r
     sel = r["selection"]
     plain_val = [t for t in sel["trials"] if t["strength"] == 0.0][0]["err_max"]
-    assert sel["best"]["err_max"] <= plain_val
-    # what the network gains (or not) on the evaluation scene, and the cost of the coarse form
-    print("gain (plain coarse error / learned error):", r["gain_error_ratio_plain_over_learned"],
-          "speedup vs fine:", r["speedup_learned_vs_fine"])
-    assert r["learned"]["error"]["max"] <= 2.0 * r["plain_coarse"]["error"]["max"]
+    assert sel["best"]["strength"] > 0.0 and sel["best"]["err_max"] < plain_val, sel
+    gain = r["gain_error_ratio_plain_over_learned"]
+    print("gain (plain coarse error / learned error):", gain, "speedup vs fine:", r["speedup_learned_vs_fine"],
+          "learned error:", r["learned"]["error"]["max"], "plain coarse error:", r["plain_coarse"]["error"]["max"])
+    # what the network gains on the evaluation scene: a smaller error than the same coarse step without it
+    assert r["learned"]["error"]["max"] < r["plain_coarse"]["error"]["max"], r["learned"]
+    # measured on a GB300 in two runs: learned 1.57e-3 / 1.02e-3 against plain coarse 1.87e-3 (the
+    # training is not bit-reproducible: atomic sums), 4.8x / 1.9x faster than the fine rollout
+    # (the selected form and how often its det F / energy fallback runs fine steps differ)
     assert r["speedup_plain_coarse_vs_fine"] > 1.5
