@@ -1,10 +1,12 @@
-"""Batched 2D scenes: many independent MLS-MPM scenes advanced by one persistent launch per substep.
+"""Batched 2D scenes: many independent MLS-MPM scenes advanced by one persistent launch per call.
 
 Each scene has its own particles, grid resolution, material (two_d.p2g's scalar ``mass``,
 ``mu_0``, ``lambda_0``), dt, gravity and walls.  The particle state of all scenes lives in one set
-of component-major arrays; ``substeps`` launches one cooperative kernel per substep (P2G, grid,
-G2P of every scene with grid-wide barriers in between), ``capture`` records a CUDA graph of many
-substeps, and ``autotune`` picks the launch shape.
+of component-major arrays, each scene's particles ordered by base cell (``scene_state`` returns
+them in the caller's order).  ``step`` runs any number of substeps in one cooperative launch (P2G,
+then per substep the grid update over each scene's box of touched nodes and G2P fused with the
+next P2G, grid-wide barriers in between), ``capture`` records such a launch in a CUDA graph, and
+``autotune`` picks the launch shape.
 """
 from __future__ import annotations
 
@@ -51,6 +53,20 @@ class Batch2D:
         C = cat("C", (2, 2), lambda c: np.zeros((c, 2, 2)))
         Jp = np.concatenate([np.asarray(s.get("Jp", np.ones(c)), dtype=np.float64).reshape(-1)
                              for s, c in zip(scenes, counts)])
+        # each scene's particles in the order of their base cell: the kernel's P2G sums the
+        # contributions of a warp's lanes that share a cell before its atomics.  perm[i] is the
+        # caller's index (within the batch) of the particle at position i.
+        perm = []
+        for s, a, c in zip(scenes, self.offsets[:-1], counts):
+            res = int(s["res"])
+            xs = x[a:a + c]
+            cell = np.clip(np.floor(xs * res - 0.5), -1, res).astype(np.int64)
+            perm.append(a + np.argsort(cell[:, 0] * (res + 2) + cell[:, 1], kind="stable"))
+        perm = np.concatenate(perm) if perm else np.zeros(0, dtype=np.int64)
+        x, v, F, C, Jp = x[perm], v[perm], F[perm], C[perm], Jp[perm]
+        self.perm = torch.as_tensor(perm, device=self.device)
+        self._inv = torch.empty_like(self.perm)
+        self._inv[self.perm] = torch.arange(n, device=self.device)
         dev = lambda a: torch.tensor(a, dtype=dtype, device=self.device)
         self.x, self.v = dev(x.T.copy()), dev(v.T.copy())
         self.F, self.C = dev(F.reshape(n, 4).T.copy()), dev(C.reshape(n, 4).T.copy())
@@ -97,7 +113,7 @@ class Batch2D:
             self._launch(nsteps)
 
     def capture(self, nsteps: int):
-        """Record `nsteps` substeps (one cooperative launch each) in a CUDA graph."""
+        """Record `nsteps` substeps (one cooperative launch) in a CUDA graph."""
         self._launch(1)
         torch.cuda.synchronize(self.device)
         g = torch.cuda.CUDAGraph()
@@ -139,11 +155,17 @@ class Batch2D:
         return int(st.value)
 
     def scene_state(self, i: int) -> Dict[str, torch.Tensor]:
+        """Scene i's state in the caller's particle order (the batch keeps it ordered by cell)."""
         a, b = int(self.offsets[i]), int(self.offsets[i + 1])
         c = b - a
-        return dict(x=self.x[:, a:b].T.contiguous(), v=self.v[:, a:b].T.contiguous(),
-                    F=self.F[:, a:b].T.reshape(c, 2, 2).contiguous(),
-                    C=self.C[:, a:b].T.reshape(c, 2, 2).contiguous(), Jp=self.Jp[a:b].clone())
+        pos = self._inv[a:b]  # where the scene's particles sit in the batch, in the caller's order
+        return dict(x=self.x[:, pos].T.contiguous(), v=self.v[:, pos].T.contiguous(),
+                    F=self.F[:, pos].T.reshape(c, 2, 2).contiguous(),
+                    C=self.C[:, pos].T.reshape(c, 2, 2).contiguous(), Jp=self.Jp[pos].clone())
+
+    def position(self, i: int, k: int) -> int:
+        """Index in the batch arrays of the caller's particle k of scene i."""
+        return int(self._inv[int(self.offsets[i]) + k])
 
 
 def random_scenes(nscenes: int = 256, seed: int = 0, n_range=(2048, 65536), res_range=(64, 256),
@@ -231,8 +253,20 @@ def main(argv=None):
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--profile-case", action="store_true",
+                    help="stable variant, 256 threads per CTA: one launch of 3 substeps, then one launch of "
+                         "--steps substeps (the one to capture with a profiler); prints the status")
     a = ap.parse_args(argv)
     sc = random_scenes(a.scenes, seed=a.seed)
+    if a.profile_case:
+        b = Batch2D(stable_variant(sc), dtype=torch.float32)
+        b.threads, b.ctas_per_sm = 256, 0
+        b.step(3)
+        torch.cuda.synchronize()
+        b.step(a.steps)
+        torch.cuda.synchronize()
+        print(json.dumps({"particles": b.n, "substeps": a.steps, "status": b.status()}))
+        return
     rep = {"as_written": measure(sc, a.steps, sequential=False), "stable_variant": measure(stable_variant(sc), a.steps)}
     print(json.dumps(rep, indent=1, default=float))
 

@@ -288,15 +288,21 @@ typedef struct ffmpm_scene2d {
 /* Workspace bytes for a batch (scene table + every scene's two grids). */
 int ffmpm_batch2d_workspace_size(const ffmpm_scene2d *scenes, int32_t nscenes, int32_t real_bytes, size_t *bytes);
 
-/* Copy the scene table into the workspace and zero the grids (synchronises `stream`). */
+/* Copy the scene table into the workspace (with each scene's parameters converted to the compute
+ * type `real_bytes`, which every later call on this workspace must pass too), empty the scenes'
+ * node boxes and zero the grids (synchronises `stream`). */
 int ffmpm_batch2d_init(const ffmpm_scene2d *scenes, int32_t nscenes, int32_t real_bytes, void *ws, size_t ws_bytes,
                        void *stream);
 
-/* `nsteps` substeps of every scene: per substep one cooperative launch that runs P2G, the grid
- * update and G2P of all scenes, separated by grid-wide barriers (two_d/p2g.py, grid_op.py, g2p.py
- * per scene).  `threads` (128/256/512) and `ctas_per_sm` (0 = as many as fit) set the launch
- * shape; the autotuner chooses them.  Particles are updated in place.  No reference counterpart
- * (the reference steps one scene at a time). */
+/* `nsteps` substeps of every scene in one cooperative launch: P2G, then per substep the grid update
+ * and G2P of all scenes (two_d/p2g.py, grid_op.py, g2p.py per scene), separated by grid-wide
+ * barriers; between substeps each particle's G2P is followed in the same pass by its next P2G.
+ * The grid update visits only the nodes inside each scene's box of touched nodes.  P2G sums the
+ * contributions of neighbouring particles with the same base cell before its atomics, which pays
+ * when each scene's particles are ordered by base cell (Batch2D orders them).  `threads`
+ * (128/256/512) and `ctas_per_sm` (0 = as many as fit) set the launch shape; the autotuner
+ * chooses them.  Particles are updated in place.  No reference counterpart (the reference steps
+ * one scene at a time). */
 int ffmpm_batch2d_substeps(int32_t nscenes, int32_t real_bytes, ffmpm_particles *P, int32_t nsteps, int32_t threads,
                            int32_t ctas_per_sm, void *ws, size_t ws_bytes, void *stream);
 
