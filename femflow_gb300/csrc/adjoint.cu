@@ -2,8 +2,9 @@
 // with the "neo_hookean" fixed-corotated stress of utils.py:95-135).
 //
 // The substep is x, v, F, C -> P2G -> grid update -> G2P -> x', v', F', C'.  Its reverse, given the
-// adjoints of x', v', F', C', runs four kernels on a dense (res+1)^3 grid:
+// adjoints of x', v', F', C', runs five kernels on a dense (res+1)^3 grid:
 //   k_adj_p2g      recompute the substep's grid (momentum, mass) from the input state
+//   k_adj_gridvel  the grid update of every node once: updated velocity (and mass) for the gathers
 //   k_adj_g2p      reverse G2P: per particle, scatter the node-velocity adjoints (one vector red per
 //                  stencil node) and form dL/dx, dL/dF of the gather and of F' = (I + dt C') F
 //   k_adj_grid     reverse grid update per node: division by mass, gravity, clamp and walls (the
@@ -13,7 +14,12 @@
 //                  for F = R S, dL/dF gains R [y]_x with (tr(S) I - S) y = axial(R^T dL/dR).
 //
 // Both node grids are float64 for float particle states too, and every node contribution is formed
-// in float64 from float factors (a product of two floats is exact in double).  The adjoints carry a
+// in float64 from float factors (a product of two floats is exact in double).  For float states,
+// the grids the particle kernels read back (updated velocities, node adjoints) are stored as float
+// pairs hi + lo (hi = the float nearest the double, lo = the float nearest the rest): a stencil
+// node's deviation from the stencil's centre node, (hi - hi_c) + (lo - lo_c), is then formed in
+// float with the accuracy of the double subtraction rounded to float (hi - hi_c is exact when the
+// two are within a factor two), without the float64 pipe.  Double states keep double grids.  The adjoints carry a
 // large, nearly uniform part (a body's bulk motion); the stress derivative needs only its variation
 // across a stencil, sum W (g_i - g) (x) dpos_i.  With float node sums, rounding that differs from
 // node to node (in the momentum and in the mass it is divided by) leaves ~1e-7 of the bulk part in
@@ -21,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 #include "internal.h"
@@ -77,6 +84,48 @@ __device__ __forceinline__ void load_state(const PView<T>& P, uint32_t p, T x[3]
   }
 }
 
+// A float64 node {x, y, z, w} as float pairs: hi = RN(v), lo = RN(v - hi), in the 32 bytes of a
+// Node4<double>.
+struct HiLo4 {
+  float4 hi, lo;
+};
+static_assert(sizeof(HiLo4) == sizeof(Node4<double>), "same slot");
+
+// Node format of the grids read back by the particle kernels: HiLo4 for float states, double
+// otherwise.
+template <typename T>
+using ReadNode = std::conditional_t<sizeof(T) == 4, HiLo4, Node4<double>>;
+
+__device__ __forceinline__ void store_node(HiLo4* g, int64_t i, double x, double y, double z, double w) {
+  HiLo4 o;
+  o.hi = make_float4(float(x), float(y), float(z), float(w));
+  o.lo = make_float4(float(x - double(o.hi.x)), float(y - double(o.hi.y)), float(z - double(o.hi.z)),
+                     float(w - double(o.hi.w)));
+  g[i] = o;
+}
+__device__ __forceinline__ void store_node(Node4<double>* g, int64_t i, double x, double y, double z, double w) {
+  g[i] = Node4<double>{x, y, z, w};
+}
+
+// Node value minus the reference node value c, per component.
+__device__ __forceinline__ void node_dev(const HiLo4& a, const HiLo4& c, float o[4]) {
+  o[0] = (a.hi.x - c.hi.x) + (a.lo.x - c.lo.x);
+  o[1] = (a.hi.y - c.hi.y) + (a.lo.y - c.lo.y);
+  o[2] = (a.hi.z - c.hi.z) + (a.lo.z - c.lo.z);
+  o[3] = (a.hi.w - c.hi.w) + (a.lo.w - c.lo.w);
+}
+__device__ __forceinline__ void node_dev(const Node4<double>& a, const Node4<double>& c, double o[4]) {
+  o[0] = a.x - c.x;
+  o[1] = a.y - c.y;
+  o[2] = a.z - c.z;
+  o[3] = a.w - c.w;
+}
+__device__ __forceinline__ double node_comp(const HiLo4& a, int d) {
+  const float h = d == 0 ? a.hi.x : d == 1 ? a.hi.y : a.hi.z, l = d == 0 ? a.lo.x : d == 1 ? a.lo.y : a.lo.z;
+  return double(h) + double(l);
+}
+__device__ __forceinline__ double node_comp(const Node4<double>& a, int d) { return d == 0 ? a.x : d == 1 ? a.y : a.z; }
+
 __device__ __forceinline__ void red_add3(Node4<double>* p, double a, double b, double c) {
   atomicAdd(&p->x, a);
   atomicAdd(&p->y, b);
@@ -120,12 +169,26 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_p2g(KParams<T> kp, PView<T>
 }
 
 // ---------------------------------------------------------------------------------------------
+// Forward grid update (three_d/grid_op.py:5-47) of every node: {updated velocity, mass}.
+template <typename G>
+__global__ void __launch_bounds__(kAdjThreads) k_adj_gridvel(KParams<double> kp, const Node4<double>* __restrict__ grid,
+                                                             G* __restrict__ gvel, int64_t nnodes) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nnodes) return;
+  const int R = kp.res + 1;
+  const int I[3] = {(int)(idx / ((int64_t)R * R)), (int)((idx / R) % R), (int)(idx % R)};
+  const Node4<double> g = grid[idx];
+  double vel[3] = {g.x, g.y, g.z};
+  grid_node<3, double>(kp, I, vel, g.w);
+  store_node(gvel, idx, vel[0], vel[1], vel[2], g.w);
+}
+
+// ---------------------------------------------------------------------------------------------
 // Reverse G2P (three_d/g2p.py:9-59).  Forward: v' = sum W vg, C' = 4 inv_dx sum W vg (x) (i - fx),
 // x' = x + dt v', F' = (I + dt C') F, with vg the updated node velocity.
 template <typename T>
-__global__ void __launch_bounds__(kAdjThreads) k_adj_g2p(KParams<T> kp, KParams<double> kd, PView<T> P,
-                                                         AView<T> Ab, uint32_t n,
-                                                         const Node4<double>* __restrict__ grid,
+__global__ void __launch_bounds__(kAdjThreads) k_adj_g2p(KParams<T> kp, PView<T> P, AView<T> Ab, uint32_t n,
+                                                         const ReadNode<T>* __restrict__ gvel,
                                                          Node4<double>* __restrict__ gadj, int32_t* status) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
@@ -161,15 +224,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_g2p(KParams<T> kp, KParams<
   //   dL/dx_d = inv_dx (sum dW_d (vb.dv_i + c4 dv_i.Cb r_i) - c4 (Cb^T sum W dv_i)_d)
   T v1[3] = {0, 0, 0}, C1[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, xacc[3] = {0, 0, 0};
   const int R = kp.res + 1;
-  double u[3];
-  {
-    const int I[3] = {b[0] + 1, b[1] + 1, b[2] + 1};
-    const Node4<double> gn = grid[((int64_t)I[0] * R + I[1]) * R + I[2]];
-    u[0] = gn.x;
-    u[1] = gn.y;
-    u[2] = gn.z;
-    grid_node<3, double>(kd, I, u, gn.w);
-  }
+  const ReadNode<T> u = gvel[((int64_t)(b[0] + 1) * R + (b[1] + 1)) * R + (b[2] + 1)];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -180,12 +235,9 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_g2p(KParams<T> kp, KParams<
         const T g0 = dw[i][0] * w[j][1] * w[k][2], g1 = w[i][0] * dw[j][1] * w[k][2],
                 g2 = w[i][0] * w[j][1] * dw[k][2];
         const T r[3] = {T(i) - fx[0], T(j) - fx[1], T(k) - fx[2]};
-        const int I[3] = {b[0] + i, b[1] + j, b[2] + k};
-        const int64_t node = ((int64_t)I[0] * R + I[1]) * R + I[2];
-        const Node4<double> gn = grid[node];
-        double veld[3] = {gn.x, gn.y, gn.z};
-        grid_node<3, double>(kd, I, veld, gn.w);
-        const T vel[3] = {T(veld[0] - u[0]), T(veld[1] - u[1]), T(veld[2] - u[2])};
+        const int64_t node = ((int64_t)(b[0] + i) * R + (b[1] + j)) * R + (b[2] + k);
+        T vel[4];
+        node_dev(gvel[node], u, vel);
         T cr[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -224,7 +276,10 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_g2p(KParams<T> kp, KParams<
 }
 
 // ---------------------------------------------------------------------------------------------
-// Reverse grid update (three_d/grid_op.py:5-47): node adjoints {dL/dvg} -> {dL/dmomentum, dL/dmass}.
+// Reverse grid update (three_d/grid_op.py:5-47): node adjoints {dL/dvg} -> {dL/dmomentum, dL/dmass},
+// written over the node's slot in the read-back format G (a node without adjoint stays all zero,
+// which reads as zero in either format).
+template <typename G>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_grid(KParams<double> kp, const Node4<double>* __restrict__ grid,
                                                           Node4<double>* __restrict__ gadj, int64_t nnodes) {
   using T = double;
@@ -272,7 +327,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_grid(KParams<double> kp, co
     o.z = vb[2];
     o.w = T(0);
   }
-  gadj[idx] = o;
+  store_node(reinterpret_cast<G*>(gadj), idx, o.x, o.y, o.z, o.w);
 }
 
 // dL/dF += dL/dR through the orthogonal polar factor R of F (F = R S): R [y]_x with
@@ -314,7 +369,7 @@ __device__ __forceinline__ void polar3_vjp(const T F[9], const T R[9], const T R
 // (on all nine entries, or on the diagonal for FFMPM_MODEL_FIXED_COROTATED).
 template <typename T>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_p2g_rev(KParams<T> kp, PView<T> P, AView<T> Ab, uint32_t n,
-                                                             const Node4<double>* __restrict__ gadj,
+                                                             const ReadNode<T>* __restrict__ gadj,
                                                              int32_t* status) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
@@ -328,13 +383,26 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_p2g_rev(KParams<T> kp, PVie
   }
   T m, mu, lam;
   lame_of(kp, P, p, m, mu, lam);
-  // The stress derivative is formed in float64 from the particle's (float or double) F: its mu / lam
-  // terms are sums over particles and substeps of <G, (F - R) F^T>, which cancel heavily, and float
-  // F - R near a rotation keeps only ~1e-7 / |F - R| relative accuracy.
-  double Fd[9], Rd[9];
+  // The stress derivative needs F - R at the working precision relative to its own size: its mu /
+  // lam terms are sums over particles and substeps of <G, (F - R) F^T>, which cancel heavily, and
+  // F - R formed as the difference of float F and float R keeps only ~1e-7 / |F - R| relative
+  // accuracy.  Float states take the small-strain form of F - R (as the forward stress does; float
+  // relative precision), and F - R from Newton's R where the strain is large (there |F - R| >~
+  // 0.02); J and the per-particle sums over the nine entries of the mu / lam terms are float64.
+  T FmR[9], Rf[9];
+  bool small = false;
+  if constexpr (sizeof(T) == 4) small = f_minus_r_small_strain3(F, FmR);
+  if (small) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) Rf[i] = F[i] - FmR[i];
+  } else {
+    polar3<T>(F, Rf, nullptr);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) FmR[i] = F[i] - Rf[i];
+  }
+  double Fd[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) Fd[i] = double(F[i]);
-  polar3<double>(Fd, Rd, nullptr);
   const double Jd = det3(Fd);
   const T Dinv = T(4) * kp.inv_dx * kp.inv_dx;
   const T s = -(kp.dt * kp.volume);
@@ -349,25 +417,26 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_p2g_rev(KParams<T> kp, PVie
       for (int c = 0; c < 3; ++c) {
         T pf = (a == c || !diag) ? sc : T(0);
 #pragma unroll
-        for (int e = 0; e < 3; ++e) pf += T(2) * mu * (F[a * 3 + e] - T(Rd[a * 3 + e])) * F[c * 3 + e];
+        for (int e = 0; e < 3; ++e) pf += T(2) * mu * FmR[a * 3 + e] * F[c * 3 + e];
         A[a * 3 + c] = s * (Dinv * pf) + m * C[a * 3 + c];
       }
   }
   const int R = kp.res + 1;
-  // pass 1: the particle's weighted node adjoints gsum = sum W g, gmsum = sum W gm
-  double gsum[3] = {0, 0, 0}, gmsum = 0;
+  // pass 1: the particle's weighted node adjoints gsum = sum W g, gmsum = sum W gm, held as the
+  // centre node's value c plus the weighted sums of the deviations g - c
+  const ReadNode<T> c = gadj[((int64_t)(b[0] + 1) * R + (b[1] + 1)) * R + (b[2] + 1)];
+  T gdev[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j)
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        const double wt = double(w[i][0] * w[j][1] * w[k][2]);
-        const Node4<double> a4 = gadj[((int64_t)(b[0] + i) * R + (b[1] + j)) * R + (b[2] + k)];
-        gsum[0] += wt * a4.x;
-        gsum[1] += wt * a4.y;
-        gsum[2] += wt * a4.z;
-        gmsum += wt * a4.w;
+        const T wt = w[i][0] * w[j][1] * w[k][2];
+        T dv[4];
+        node_dev(gadj[((int64_t)(b[0] + i) * R + (b[1] + j)) * R + (b[2] + k)], c, dv);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) gdev[a] += wt * dv[a];
       }
   // pass 2: Abar = sum W (g - gsum) (x) dpos (the same sum, since sum W dpos = 0, without the
   // cancellation of the uniform part of g) and the weight derivatives for dL/dx, also on the
@@ -384,20 +453,23 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_p2g_rev(KParams<T> kp, PVie
         const T g0 = dw[i][0] * w[j][1] * w[k][2], g1 = w[i][0] * dw[j][1] * w[k][2],
                 g2 = w[i][0] * w[j][1] * dw[k][2];
         const T dp[3] = {(T(i) - fx[0]) * kp.dx, (T(j) - fx[1]) * kp.dx, (T(k) - fx[2]) * kp.dx};
-        const Node4<double> a4 = gadj[((int64_t)(b[0] + i) * R + (b[1] + j)) * R + (b[2] + k)];
-        const T gb[3] = {T(a4.x - gsum[0]), T(a4.y - gsum[1]), T(a4.z - gsum[2])};
-        T term = T(a4.w - gmsum) * m;
+        T dv[4];
+        node_dev(gadj[((int64_t)(b[0] + i) * R + (b[1] + j)) * R + (b[2] + k)], c, dv);
+        const T gb[3] = {dv[0] - gdev[0], dv[1] - gdev[1], dv[2] - gdev[2]};
+        T term = (dv[3] - gdev[3]) * m;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
           const T gc = wt * gb[a];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) Abar[a * 3 + c] += gc * dp[c];
+          for (int e = 0; e < 3; ++e) Abar[a * 3 + e] += gc * dp[e];
           term += gb[a] * (m * v[a] + A[a * 3 + 0] * dp[0] + A[a * 3 + 1] * dp[1] + A[a * 3 + 2] * dp[2]);
         }
         xacc[0] += g0 * term;
         xacc[1] += g1 * term;
         xacc[2] += g2 * term;
       }
+  const double gsum[3] = {node_comp(c, 0) + double(gdev[0]), node_comp(c, 1) + double(gdev[1]),
+                          node_comp(c, 2) + double(gdev[2])};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const size_t ix = Ab.at(p, d, 3);
@@ -406,43 +478,44 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_p2g_rev(KParams<T> kp, PVie
   }
   // stress: G = dL/dPF; sG = <G, dPF/d(lam(J-1)J)>, the sum of G's entries (the reference's stress)
   // or its trace (the textbook model)
-  double G[9], Fb[9], sG = 0;
+  T G[9], Fb[9];
+  double sG = 0;
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
-    G[i] = double(s * Dinv) * double(Abar[i]);
-    if (!diag || i % 4 == 0) sG += G[i];
+    G[i] = (s * Dinv) * Abar[i];
+    if (!diag || i % 4 == 0) sG += double(G[i]);
     Ab.C[Ab.at(p, i, 9)] = m * Abar[i];
-    Fb[i] = double(Ab.F[Ab.at(p, i, 9)]);
+    Fb[i] = Ab.F[Ab.at(p, i, 9)];
   }
-  double Cof[9], Rb[9];
-  cofactor3(Fd, Cof);
+  T Cof[9], Rb[9];
+  cofactor3(F, Cof);
   double dmu = 0;
-  const double mud = double(mu), lj = double(lam) * (2.0 * Jd - 1.0) * sG;
+  const T lj = T(double(lam) * (2.0 * Jd - 1.0) * sG);
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      double gf = 0, gtfr = 0, mfr = 0;
+      T gf = 0, gtfr = 0, mfr = 0;
 #pragma unroll
       for (int e = 0; e < 3; ++e) {
-        gf += G[a * 3 + e] * Fd[e * 3 + c];                      // (G F)[a][c]
-        gtfr += G[e * 3 + a] * (Fd[e * 3 + c] - Rd[e * 3 + c]);  // (G^T (F - R))[a][c]
-        mfr += (Fd[a * 3 + e] - Rd[a * 3 + e]) * Fd[c * 3 + e];  // ((F - R) F^T)[a][c]
+        gf += G[a * 3 + e] * F[e * 3 + c];       // (G F)[a][c]
+        gtfr += G[e * 3 + a] * FmR[e * 3 + c];   // (G^T (F - R))[a][c]
+        mfr += FmR[a * 3 + e] * F[c * 3 + e];    // ((F - R) F^T)[a][c]
       }
-      Fb[a * 3 + c] += 2.0 * mud * (gf + gtfr) + lj * Cof[a * 3 + c];
-      Rb[a * 3 + c] = -2.0 * mud * gf;
-      dmu += G[a * 3 + c] * mfr;
+      Fb[a * 3 + c] += T(2) * mu * (gf + gtfr) + lj * Cof[a * 3 + c];
+      Rb[a * 3 + c] = -T(2) * mu * gf;
+      dmu += double(G[a * 3 + c]) * double(mfr);
     }
-  polar3_vjp(Fd, Rd, Rb, Fb);
+  polar3_vjp<T>(F, Rf, Rb, Fb);
 #pragma unroll
-  for (int i = 0; i < 9; ++i) Ab.F[Ab.at(p, i, 9)] = T(Fb[i]);
+  for (int i = 0; i < 9; ++i) Ab.F[Ab.at(p, i, 9)] = Fb[i];
   if (Ab.mu0) Ab.mu0[p] += double(kp.hardening) * 2.0 * dmu;
   if (Ab.lam0) Ab.lam0[p] += double(kp.hardening) * (Jd - 1.0) * Jd * sG;
 }
 
 struct AdjLayout {
   int64_t nnodes = 0;
-  size_t off_grid = 0, off_gadj = 0, total = 0;
+  size_t off_grid = 0, off_gvel = 0, off_gadj = 0, total = 0;
 };
 
 bool adj_layout(const ffmpm_params& p, AdjLayout* L) {
@@ -451,7 +524,8 @@ bool adj_layout(const ffmpm_params& p, AdjLayout* L) {
   L->nnodes = R * R * R;
   const size_t nb = sizeof(Node4<double>) * L->nnodes;  // float64 node grids for either real type
   L->off_grid = sizeof(WsHeader);
-  L->off_gadj = (L->off_grid + nb + 255) / 256 * 256;
+  L->off_gvel = (L->off_grid + nb + 255) / 256 * 256;
+  L->off_gadj = (L->off_gvel + nb + 255) / 256 * 256;
   L->total = (L->off_gadj + nb + 255) / 256 * 256;
   return true;
 }
@@ -466,6 +540,7 @@ int run_adjoint(const ffmpm_params& p, const AdjLayout& L, const ffmpm_particles
   auto* hdr = reinterpret_cast<WsHeader*>(ws);
   const KParams<double> kd = kparams<double>(p);
   auto* grid = reinterpret_cast<Node4<double>*>(ws + L.off_grid);
+  auto* gvel = reinterpret_cast<Node4<double>*>(ws + L.off_gvel);
   auto* gadj = reinterpret_cast<Node4<double>*>(ws + L.off_gadj);
   const size_t nb = sizeof(Node4<double>) * L.nnodes;
   cudaMemsetAsync(grid, 0, nb, s);
@@ -474,9 +549,11 @@ int run_adjoint(const ffmpm_params& p, const AdjLayout& L, const ffmpm_particles
   const int pg = (int)((n + kAdjThreads - 1) / kAdjThreads);
   const int ng = (int)((L.nnodes + kAdjThreads - 1) / kAdjThreads);
   k_adj_p2g<T><<<pg, kAdjThreads, 0, s>>>(kp, pv, n, grid, &hdr->status);
-  k_adj_g2p<T><<<pg, kAdjThreads, 0, s>>>(kp, kd, pv, av, n, grid, gadj, &hdr->status);
-  k_adj_grid<<<ng, kAdjThreads, 0, s>>>(kd, grid, gadj, L.nnodes);
-  k_adj_p2g_rev<T><<<pg, kAdjThreads, 0, s>>>(kp, pv, av, n, gadj, &hdr->status);
+  using G = ReadNode<T>;
+  k_adj_gridvel<G><<<ng, kAdjThreads, 0, s>>>(kd, grid, reinterpret_cast<G*>(gvel), L.nnodes);
+  k_adj_g2p<T><<<pg, kAdjThreads, 0, s>>>(kp, pv, av, n, reinterpret_cast<const G*>(gvel), gadj, &hdr->status);
+  k_adj_grid<G><<<ng, kAdjThreads, 0, s>>>(kd, grid, gadj, L.nnodes);
+  k_adj_p2g_rev<T><<<pg, kAdjThreads, 0, s>>>(kp, pv, av, n, reinterpret_cast<const G*>(gadj), &hdr->status);
   return cudaGetLastError() == cudaSuccess ? FFMPM_OK : FFMPM_ERR_CUDA;
 }
 

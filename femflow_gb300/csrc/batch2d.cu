@@ -49,7 +49,7 @@ static_assert(sizeof(BatchHeader) == 256, "one 256-byte line");
 template <typename T>
 struct SceneK {
   T dx, inv_dx, dt, gravity, volume, hardening, mass, mu0, lam0, v_allowed;
-  int res, model, wall_mode;
+  int res, model, wall_mode, wall_lo, wall_hi;
 };
 
 template <typename T>
@@ -68,6 +68,7 @@ __host__ __device__ inline SceneK<T> scene_k(const ffmpm_scene2d& s) {
   k.res = s.res;
   k.model = s.model;
   k.wall_mode = s.wall_mode;
+  wall_band_2d(s.res, &k.wall_lo, &k.wall_hi);
   return k;
 }
 
@@ -188,6 +189,8 @@ __device__ __forceinline__ KParams<T> scene_kparams(const SceneK<T>& s) {
   k.res = s.res;
   k.model = s.model;
   k.wall_mode = s.wall_mode;
+  k.wall_lo = s.wall_lo;
+  k.wall_hi = s.wall_hi;
   k.variant = 0;
   return k;
 }

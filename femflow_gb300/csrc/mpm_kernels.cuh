@@ -28,6 +28,9 @@ template <typename T>
 struct KParams {
   T dx, inv_dx, dt, gravity, volume, hardening, mass, mu0, lam0, v_allowed;
   int res, model, wall_mode, variant;
+  // 2D reference walls as node-index bounds (wall_band_2d): I / res < 0.05 <=> I < wall_lo and
+  // I / res > 1 - 0.05 <=> I > wall_hi
+  int wall_lo = 0, wall_hi = 0;
   // planar colliders: {point, normal'} in float64 with the plane rule already applied to the normal
   int n_planes = 0;
   double dx64 = 0.0;
@@ -74,6 +77,26 @@ struct PView {
   }
 };
 
+// The 2D reference walls (two_d/grid_op.py:13-19) compare the node coordinate I / res, computed in
+// float64, with 0.05 and 1 - 0.05.  Correctly rounded I / res grows with I, so each comparison
+// holds on a prefix or a suffix of 0..res: the first index with I / res >= 0.05 and the last with
+// I / res <= 1 - 0.05, found here with the same float64 arithmetic, replace the two divisions per
+// node.
+__host__ __device__ inline void wall_band_2d(int res, int* lo, int* hi) {
+  *lo = res + 1;
+  for (int i = 0; i <= res; ++i)
+    if (!(double(i) / double(res) < 0.05)) {
+      *lo = i;
+      break;
+    }
+  *hi = -1;
+  for (int i = res; i >= 0; --i)
+    if (!(double(i) / double(res) > 1.0 - 0.05)) {
+      *hi = i;
+      break;
+    }
+}
+
 // Kernel parameters and particle view of the C-ABI structs (host side).
 template <typename T>
 inline KParams<T> kparams(const ffmpm_params& p) {
@@ -92,6 +115,7 @@ inline KParams<T> kparams(const ffmpm_params& p) {
   k.model = p.model;
   k.wall_mode = p.wall_mode;
   k.variant = p.variant;
+  wall_band_2d(p.res, &k.wall_lo, &k.wall_hi);
   k.n_planes = std::max(0, std::min(int(p.n_planes), FFMPM_MAX_PLANES));
   k.dx64 = p.dx;
   for (int q = 0; q < k.n_planes; ++q) {
@@ -1439,9 +1463,10 @@ __device__ __forceinline__ void grid_node(const KParams<T>& kp, const int I[DIM]
       vel[1] = vel[1] / m;
       vel[1] += kp.dt * kp.gravity;
       if (kp.wall_mode == FFMPM_WALLS_REFERENCE) {
-        const double xx = double(I[0]) / double(kp.res), yy = double(I[1]) / double(kp.res);
-        if (xx < 0.05 || xx > 1.0 - 0.05 || yy > 1.0 - 0.05) vel[0] = vel[1] = T(0);
-        if (yy < 0.05) vel[1] = vel[1] > T(0) ? vel[1] : T(0);
+        // x = I0 / res, y = I1 / res: x < 0.05, x > 0.95 or y > 0.95 stop the node; y < 0.05 keeps
+        // only an upward velocity
+        if (I[0] < kp.wall_lo || I[0] > kp.wall_hi || I[1] > kp.wall_hi) vel[0] = vel[1] = T(0);
+        if (I[1] < kp.wall_lo) vel[1] = vel[1] > T(0) ? vel[1] : T(0);
       } else {
         bool near = I[0] < 3 || I[0] > kp.res - 3 || I[1] < 3 || I[1] > kp.res - 3;
         if (near) vel[0] = vel[1] = T(0);
