@@ -1,5 +1,6 @@
 // Reverse mode of one 3D MLS-MPM substep (the derivative of solve_mls_mpm_3d, mls_mpm.py:40-79,
-// with the "neo_hookean" fixed-corotated stress of utils.py:95-135).
+// with the "neo_hookean" fixed-corotated stress of utils.py:95-135), and of the 2D substep
+// (two_d/*.py with utils.py:52-92) further below.
 //
 // The substep is x, v, F, C -> P2G -> grid update -> G2P -> x', v', F', C'.  Its reverse, given the
 // adjoints of x', v', F', C', runs five kernels on a dense (res+1)^3 grid:
@@ -513,15 +514,344 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_p2g_rev(KParams<T> kp, PVie
   if (Ab.lam0) Ab.lam0[p] += double(kp.hardening) * (Jd - 1.0) * Jd * sG;
 }
 
+
+// ---------------------------------------------------------------------------------------------
+// 2D (two_d/p2g.py:11-76, two_d/grid_op.py:5-24, two_d/g2p.py:5-47) for the elastic models: the
+// same five kernels over a dense (res+1)^2 grid, with the 0.05 wall band (the y < 0.05 rule keeps
+// v_y only where it is positive, and passes its adjoint only there), no velocity clamp, and the
+// closed-form rotation R of linear_algebra.py:97-116, c = x/d, s = y/d, d = |(x, y)| + 1e-10 with
+// x = F00 + F11, y = F10 - F01.  Jp does not feed back for these models.  2D grids are small, so
+// every grid is float64 and read back as such; F - R comes from the float64 rotation.
+template <typename T>
+__device__ __forceinline__ bool stencil2(const KParams<T>& kp, const T x[2], int b[2], T fx[2], T w[3][2],
+                                         T dw[3][2]) {
+  bool ok = true;
+#pragma unroll
+  for (int d = 0; d < 2; ++d) ok = ok && base_of(x[d], kp.inv_dx, kp.res, b[d], fx[d]);
+  if (!ok) return false;
+#pragma unroll
+  for (int d = 0; d < 2; ++d) {
+    T ww[3];
+    bspline(fx[d], ww);
+    w[0][d] = ww[0];
+    w[1][d] = ww[1];
+    w[2][d] = ww[2];
+    dw[0][d] = fx[d] - T(1.5);
+    dw[1][d] = T(-2) * (fx[d] - T(1));
+    dw[2][d] = fx[d] - T(0.5);
+  }
+  return true;
+}
+
+template <typename T>
+__device__ __forceinline__ void load_state2(const PView<T>& P, uint32_t p, T x[2], T v[2], T F[4], T C[4]) {
+#pragma unroll
+  for (int d = 0; d < 2; ++d) {
+    if (x) x[d] = P.x[P.at(p, d, 2)];
+    if (v) v[d] = P.v[P.at(p, d, 2)];
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (F) F[i] = P.F[P.at(p, i, 4)];
+    if (C) C[i] = P.C[P.at(p, i, 4)];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kAdjThreads) k_adj2_p2g(KParams<T> kp, PView<T> P, uint32_t n,
+                                                          Node4<double>* __restrict__ grid, int32_t* status) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  T x[2], v[2], F[4], C[4];
+  load_state2(P, p, x, v, F, C);
+  int b[2];
+  T fx[2], w[3][2], dw[3][2];
+  if (!stencil2(kp, x, b, fx, w, dw)) {
+    raise_status(status, FFMPM_STATUS_OOB);
+    return;
+  }
+  T m, mu, lam;
+  lame_of(kp, P, p, m, mu, lam);
+  T A[4];
+  affine_of<2, T>(kp, F, C, m, mu, lam, A, nullptr);
+  const int R = kp.res + 1;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double wt = double(w[i][0]) * double(w[j][1]);
+      const T d0 = (T(i) - fx[0]) * kp.dx, d1 = (T(j) - fx[1]) * kp.dx;
+      const double q0 = double(m) * double(v[0]) + double(A[0] * d0 + A[1] * d1);
+      const double q1 = double(m) * double(v[1]) + double(A[2] * d0 + A[3] * d1);
+      atomic_add4(&grid[(int64_t)(b[0] + i) * R + (b[1] + j)], wt * q0, wt * q1, 0.0, wt * double(m));
+    }
+}
+
+__global__ void __launch_bounds__(kAdjThreads) k_adj2_gridvel(KParams<double> kp, const Node4<double>* __restrict__ grid,
+                                                              Node4<double>* __restrict__ gvel, int64_t nnodes) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nnodes) return;
+  const int R = kp.res + 1;
+  const int I[2] = {(int)(idx / R), (int)(idx % R)};
+  const Node4<double> g = grid[idx];
+  double vel[3] = {g.x, g.y, 0.0};
+  grid_node<2, double>(kp, I, vel, g.w);
+  gvel[idx] = Node4<double>{vel[0], vel[1], 0.0, g.w};
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kAdjThreads) k_adj2_g2p(KParams<T> kp, PView<T> P, AView<T> Ab, uint32_t n,
+                                                          const Node4<double>* __restrict__ gvel,
+                                                          Node4<double>* __restrict__ gadj, int32_t* status) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  T x[2], F[4];
+  load_state2<T>(P, p, x, nullptr, F, nullptr);
+  int b[2];
+  T fx[2], w[3][2], dw[3][2];
+  if (!stencil2(kp, x, b, fx, w, dw)) {
+    raise_status(status, FFMPM_STATUS_OOB);
+    return;
+  }
+  T xb[2], vb[2], Fb1[4], Cb[4];
+#pragma unroll
+  for (int d = 0; d < 2; ++d) {
+    xb[d] = Ab.x[Ab.at(p, d, 2)];
+    vb[d] = Ab.v[Ab.at(p, d, 2)] + kp.dt * xb[d];  // x' = x + dt v'
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    Fb1[i] = Ab.F[Ab.at(p, i, 4)];
+    Cb[i] = Ab.C[Ab.at(p, i, 4)];
+  }
+  // C' enters F' = (I + dt C') F: dL/dC' += dt dL/dF' F^T
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) Cb[a * 2 + c] += kp.dt * (Fb1[a * 2 + 0] * F[c * 2 + 0] + Fb1[a * 2 + 1] * F[c * 2 + 1]);
+  const T c4 = T(4) * kp.inv_dx;
+  // node velocities relative to the centre node's u, as in 3D: the u terms of dL/dx cancel
+  T v1[2] = {0, 0}, C1[4] = {0, 0, 0, 0}, xacc[2] = {0, 0};
+  const int R = kp.res + 1;
+  const Node4<double> u = gvel[(int64_t)(b[0] + 1) * R + (b[1] + 1)];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const T wt = w[i][0] * w[j][1];
+      const T g0 = dw[i][0] * w[j][1], g1 = w[i][0] * dw[j][1];
+      const T r[2] = {T(i) - fx[0], T(j) - fx[1]};
+      const int64_t node = (int64_t)(b[0] + i) * R + (b[1] + j);
+      const Node4<double> gn = gvel[node];
+      const T vel[2] = {T(gn.x - u.x), T(gn.y - u.y)};
+      T cr[2];
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        v1[a] += wt * vel[a];
+        C1[a * 2 + 0] += wt * vel[a] * r[0];
+        C1[a * 2 + 1] += wt * vel[a] * r[1];
+        cr[a] = Cb[a * 2 + 0] * r[0] + Cb[a * 2 + 1] * r[1];
+      }
+      const T term = vb[0] * vel[0] + vb[1] * vel[1] + c4 * (vel[0] * cr[0] + vel[1] * cr[1]);
+      xacc[0] += g0 * term;
+      xacc[1] += g1 * term;
+      const double wd = double(wt);
+      atomicAdd(&gadj[node].x, wd * (double(vb[0]) + double(c4 * cr[0])));
+      atomicAdd(&gadj[node].y, wd * (double(vb[1]) + double(c4 * cr[1])));
+    }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) C1[i] *= c4;
+#pragma unroll
+  for (int d = 0; d < 2; ++d) {
+    const T ct = Cb[0 * 2 + d] * v1[0] + Cb[1 * 2 + d] * v1[1];
+    Ab.x[Ab.at(p, d, 2)] = xb[d] + kp.inv_dx * (xacc[d] - c4 * ct);
+  }
+  // dL/dF = (I + dt C')^T dL/dF'
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+      Ab.F[Ab.at(p, a * 2 + c, 4)] =
+          Fb1[a * 2 + c] + kp.dt * (C1[0 * 2 + a] * Fb1[0 * 2 + c] + C1[1 * 2 + a] * Fb1[1 * 2 + c]);
+}
+
+// Reverse 2D grid update: the band's stopped nodes and the clipped v_y pass nothing, then the
+// division by mass.
+__global__ void __launch_bounds__(kAdjThreads) k_adj2_grid(KParams<double> kp, const Node4<double>* __restrict__ grid,
+                                                           Node4<double>* __restrict__ gadj, int64_t nnodes) {
+  using T = double;
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nnodes) return;
+  Node4<double> a = gadj[idx];
+  if (a.x == T(0) && a.y == T(0)) return;
+  const int R = kp.res + 1;
+  const int I[2] = {(int)(idx / R), (int)(idx % R)};
+  const Node4<double> g = grid[idx];
+  T vb[2] = {a.x, a.y};
+  const T gp[2] = {g.x, g.y};
+  const T m = g.w;
+  if (m > T(0)) {
+    if (kp.wall_mode == FFMPM_WALLS_REFERENCE) {
+      if (I[0] < kp.wall_lo || I[0] > kp.wall_hi || I[1] > kp.wall_hi) vb[0] = vb[1] = T(0);
+      if (I[1] < kp.wall_lo && !(gp[1] / m + kp.dt * kp.gravity > T(0))) vb[1] = T(0);
+    } else {
+      const bool near = I[0] < 3 || I[0] > kp.res - 3 || I[1] < 3 || I[1] > kp.res - 3;
+      if (near) vb[0] = vb[1] = T(0);
+    }
+  }
+  for (int q = 0; q < kp.n_planes; ++q)
+    if (behind_plane<2, double>(kp, I, q)) vb[0] = vb[1] = T(0);
+  Node4<double> o;
+  if (m > T(0)) {
+    const T im = T(1) / m;
+    o = Node4<double>{vb[0] * im, vb[1] * im, T(0), -(vb[0] * gp[0] + vb[1] * gp[1]) * im * im};
+  } else {
+    o = Node4<double>{vb[0], vb[1], T(0), T(0)};
+  }
+  gadj[idx] = o;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kAdjThreads) k_adj2_p2g_rev(KParams<T> kp, PView<T> P, AView<T> Ab, uint32_t n,
+                                                              const Node4<double>* __restrict__ gadj,
+                                                              int32_t* status) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  T x[2], v[2], F[4], C[4];
+  load_state2(P, p, x, v, F, C);
+  int b[2];
+  T fx[2], w[3][2], dw[3][2];
+  if (!stencil2(kp, x, b, fx, w, dw)) {
+    raise_status(status, FFMPM_STATUS_OOB);
+    return;
+  }
+  T m, mu, lam;
+  lame_of(kp, P, p, m, mu, lam);
+  // the rotation in float64 (F - R at the working precision relative to its size)
+  double Fd[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) Fd[i] = double(F[i]);
+  const double rx = Fd[0] + Fd[3], ry = Fd[2] - Fd[1];
+  const double rr = sqrt(rx * rx + ry * ry), dd = rr + 1e-10;
+  const double cth = rx / dd, sth = ry / dd;
+  const double Rd[4] = {cth, -sth, sth, cth};
+  T FmR[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) FmR[i] = T(Fd[i] - Rd[i]);
+  const double Jd = Fd[0] * Fd[3] - Fd[1] * Fd[2];
+  const T Dinv = T(4) * kp.inv_dx * kp.inv_dx;
+  const T s = -(kp.dt * kp.volume);
+  const bool diag = kp.model == FFMPM_MODEL_FIXED_COROTATED;
+  T A[4];
+  {
+    const T J = T(Jd);
+    const T sc = lam * (J - T(1)) * J;
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        T pf = (a == c || !diag) ? sc : T(0);
+        pf += T(2) * mu * FmR[a * 2 + 0] * F[c * 2 + 0];
+        pf += T(2) * mu * FmR[a * 2 + 1] * F[c * 2 + 1];
+        A[a * 2 + c] = s * (Dinv * pf) + m * C[a * 2 + c];
+      }
+  }
+  const int R = kp.res + 1;
+  // pass 1: gsum = sum W g, gmsum = sum W gm as the centre node's value plus deviation sums
+  const Node4<double> c0 = gadj[(int64_t)(b[0] + 1) * R + (b[1] + 1)];
+  T gdev[3] = {T(0), T(0), T(0)};
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const T wt = w[i][0] * w[j][1];
+      const Node4<double> a4 = gadj[(int64_t)(b[0] + i) * R + (b[1] + j)];
+      gdev[0] += wt * T(a4.x - c0.x);
+      gdev[1] += wt * T(a4.y - c0.y);
+      gdev[2] += wt * T(a4.w - c0.w);
+    }
+  // pass 2: Abar = sum W (g - gsum) (x) dpos and the weight derivatives for dL/dx (see 3D)
+  T Abar[4] = {0, 0, 0, 0}, xacc[2] = {0, 0};
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const T wt = w[i][0] * w[j][1];
+      const T g0 = dw[i][0] * w[j][1], g1 = w[i][0] * dw[j][1];
+      const T dp[2] = {(T(i) - fx[0]) * kp.dx, (T(j) - fx[1]) * kp.dx};
+      const Node4<double> a4 = gadj[(int64_t)(b[0] + i) * R + (b[1] + j)];
+      const T gb[2] = {T(a4.x - c0.x) - gdev[0], T(a4.y - c0.y) - gdev[1]};
+      T term = (T(a4.w - c0.w) - gdev[2]) * m;
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        const T gc = wt * gb[a];
+        Abar[a * 2 + 0] += gc * dp[0];
+        Abar[a * 2 + 1] += gc * dp[1];
+        term += gb[a] * (m * v[a] + A[a * 2 + 0] * dp[0] + A[a * 2 + 1] * dp[1]);
+      }
+      xacc[0] += g0 * term;
+      xacc[1] += g1 * term;
+    }
+  const double gsum[2] = {c0.x + double(gdev[0]), c0.y + double(gdev[1])};
+#pragma unroll
+  for (int d = 0; d < 2; ++d) {
+    const size_t ix = Ab.at(p, d, 2);
+    Ab.x[ix] = Ab.x[ix] + kp.inv_dx * xacc[d];
+    Ab.v[ix] = T(double(m) * gsum[d]);
+  }
+  double G[4], Fb[4], sG = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    G[i] = double(s * Dinv) * double(Abar[i]);
+    if (!diag || i % 3 == 0) sG += G[i];
+    Ab.C[Ab.at(p, i, 4)] = m * Abar[i];
+    Fb[i] = double(Ab.F[Ab.at(p, i, 4)]);
+  }
+  const double Cof[4] = {Fd[3], -Fd[2], -Fd[1], Fd[0]};
+  const double mud = double(mu), lj = double(lam) * (2.0 * Jd - 1.0) * sG;
+  double Rb[4], dmu = 0;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const double fmr0 = double(FmR[0 * 2 + c]), fmr1 = double(FmR[1 * 2 + c]);
+      const double gf = G[a * 2 + 0] * Fd[0 * 2 + c] + G[a * 2 + 1] * Fd[1 * 2 + c];
+      const double gtfr = G[0 * 2 + a] * fmr0 + G[1 * 2 + a] * fmr1;
+      const double mfr = double(FmR[a * 2 + 0]) * Fd[c * 2 + 0] + double(FmR[a * 2 + 1]) * Fd[c * 2 + 1];
+      Fb[a * 2 + c] += 2.0 * mud * (gf + gtfr) + lj * Cof[a * 2 + c];
+      Rb[a * 2 + c] = -2.0 * mud * gf;
+      dmu += G[a * 2 + c] * mfr;
+    }
+  // through the rotation: cb, sb of R = [[c, -s], [s, c]], then c(x, y), s(x, y)
+  {
+    const double cb = Rb[0] + Rb[3], sb = Rb[2] - Rb[1];
+    const double k = 1.0 / (rr * dd * dd);
+    const double dcx = 1.0 / dd - rx * rx * k, dcy = -rx * ry * k;
+    const double dsx = -rx * ry * k, dsy = 1.0 / dd - ry * ry * k;
+    const double xb = cb * dcx + sb * dsx, yb = cb * dcy + sb * dsy;
+    if (rr > 0.0) {
+      Fb[0] += xb;
+      Fb[3] += xb;
+      Fb[2] += yb;
+      Fb[1] -= yb;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) Ab.F[Ab.at(p, i, 4)] = T(Fb[i]);
+  if (Ab.mu0) Ab.mu0[p] += double(kp.hardening) * 2.0 * dmu;
+  if (Ab.lam0) Ab.lam0[p] += double(kp.hardening) * (Jd - 1.0) * Jd * sG;
+}
+
 struct AdjLayout {
   int64_t nnodes = 0;
   size_t off_grid = 0, off_gvel = 0, off_gadj = 0, total = 0;
 };
 
 bool adj_layout(const ffmpm_params& p, AdjLayout* L) {
-  if (p.dim != 3 || (p.real_bytes != 4 && p.real_bytes != 8) || p.res < 3 || p.res > 1024) return false;
+  if ((p.dim != 2 && p.dim != 3) || (p.real_bytes != 4 && p.real_bytes != 8) || p.res < 3) return false;
+  if (p.res > (p.dim == 3 ? 1024 : 16384)) return false;
   const int64_t R = p.res + 1;
-  L->nnodes = R * R * R;
+  L->nnodes = p.dim == 3 ? R * R * R : R * R;
   const size_t nb = sizeof(Node4<double>) * L->nnodes;  // float64 node grids for either real type
   L->off_grid = sizeof(WsHeader);
   L->off_gvel = (L->off_grid + nb + 255) / 256 * 256;
@@ -548,6 +878,14 @@ int run_adjoint(const ffmpm_params& p, const AdjLayout& L, const ffmpm_particles
   const uint32_t n = (uint32_t)P.n;
   const int pg = (int)((n + kAdjThreads - 1) / kAdjThreads);
   const int ng = (int)((L.nnodes + kAdjThreads - 1) / kAdjThreads);
+  if (p.dim == 2) {
+    k_adj2_p2g<T><<<pg, kAdjThreads, 0, s>>>(kp, pv, n, grid, &hdr->status);
+    k_adj2_gridvel<<<ng, kAdjThreads, 0, s>>>(kd, grid, gvel, L.nnodes);
+    k_adj2_g2p<T><<<pg, kAdjThreads, 0, s>>>(kp, pv, av, n, gvel, gadj, &hdr->status);
+    k_adj2_grid<<<ng, kAdjThreads, 0, s>>>(kd, grid, gadj, L.nnodes);
+    k_adj2_p2g_rev<T><<<pg, kAdjThreads, 0, s>>>(kp, pv, av, n, gadj, &hdr->status);
+    return cudaGetLastError() == cudaSuccess ? FFMPM_OK : FFMPM_ERR_CUDA;
+  }
   k_adj_p2g<T><<<pg, kAdjThreads, 0, s>>>(kp, pv, n, grid, &hdr->status);
   using G = ReadNode<T>;
   k_adj_gridvel<G><<<ng, kAdjThreads, 0, s>>>(kd, grid, reinterpret_cast<G*>(gvel), L.nnodes);
@@ -567,7 +905,7 @@ extern "C" {
 int ffmpm_adjoint_workspace_size(const ffmpm_params* p, int64_t n, size_t* bytes) {
   AdjLayout L;
   if (!p || !bytes || n < 0) return FFMPM_ERR_BADARG;
-  if (p->dim != 3) return FFMPM_ERR_UNSUPPORTED;
+  if (p->dim != 2 && p->dim != 3) return FFMPM_ERR_UNSUPPORTED;
   if (!adj_layout(*p, &L)) return FFMPM_ERR_BADARG;
   *bytes = L.total;
   return FFMPM_OK;
@@ -576,7 +914,8 @@ int ffmpm_adjoint_workspace_size(const ffmpm_params* p, int64_t n, size_t* bytes
 int ffmpm_substep_adjoint(const ffmpm_params* p, const ffmpm_particles* P, ffmpm_adjoint* A, void* ws,
                           size_t ws_bytes, void* stream) {
   if (!p || !P || !A || P->n < 0 || P->n > int64_t(0x7FFFFFFF)) return FFMPM_ERR_BADARG;
-  if (p->dim != 3 || (p->model != FFMPM_MODEL_NEO_HOOKEAN && p->model != FFMPM_MODEL_FIXED_COROTATED))
+  if ((p->dim != 2 && p->dim != 3) ||
+      (p->model != FFMPM_MODEL_NEO_HOOKEAN && p->model != FFMPM_MODEL_FIXED_COROTATED))
     return FFMPM_ERR_UNSUPPORTED;
   if (p->wall_mode != FFMPM_WALLS_REFERENCE && p->wall_mode != FFMPM_WALLS_STICKY3) return FFMPM_ERR_BADARG;
   AdjLayout L;

@@ -1,8 +1,9 @@
-"""Differentiable 3D MLS-MPM rollouts with a hand-written adjoint.
+"""Differentiable 3D and 2D MLS-MPM rollouts with a hand-written adjoint.
 
 ``simulate(x0, v0, mu_0, lambda_0, cfg)`` runs ``cfg.steps`` substeps of the 3D solver
-(``solve_mls_mpm_3d``, femflow/solvers/mpm/mls_mpm.py:40-79; model "neo_hookean" as the reference,
-or the textbook "fixed_corotated" stress) on the GPU and
+(``solve_mls_mpm_3d``, femflow/solvers/mpm/mls_mpm.py:40-79) or, for [n, 2] states, of the 2D
+substep (femflow/solvers/mpm/two_d/*.py); model "neo_hookean" as the reference, or the textbook
+"fixed_corotated" stress.  It runs on the GPU and
 returns the final x, v, F, C as tensors that carry gradients back to x0, v0, F0, C0 and the
 per-particle Lamé parameters.  Backward is the reverse-mode sweep of ``ffmpm_substep_adjoint``:
 
@@ -10,9 +11,10 @@ per-particle Lamé parameters.  Backward is the reverse-mode sweep of ``ffmpm_su
 * backward walks the segments last to first: it re-runs a segment's substeps from its checkpoint,
   keeping each intermediate state, then applies the adjoint substeps in reverse order.
 
-Memory is ``steps / K`` checkpoints plus ``K`` states of one segment (24 reals per particle each);
-compute is two forward passes plus one adjoint pass.  The state is held component-major
-([24, n]: x 0-2, v 3-5, F 6-14, C 15-23) so every kernel access is coalesced.
+Memory is ``steps / K`` checkpoints plus ``K`` states of one segment (24 reals per particle each
+in 3D, 12 in 2D); compute is two forward passes plus one adjoint pass.  The state is held
+component-major ([24, n]: x 0-2, v 3-5, F 6-14, C 15-23; 2D [12, n]: x 0-1, v 2-3, F 4-7,
+C 8-11) so every kernel access is coalesced.
 
 Gradients with respect to Young's modulus and Poisson's ratio follow by autograd through
 ``lame(E, nu)`` (femflow/numerics/fem.py:1-6), written with torch ops.
@@ -50,30 +52,38 @@ def lame(E_mod, nu):
     return E_mod / (2 * (1 + nu)), E_mod * nu / ((1 + nu) * (1 - 2 * nu))
 
 
+def _rows(dim: int):
+    """Row offsets of x, v, F, C in the component-major buffer, and its row count."""
+    return (0, dim, 2 * dim, 2 * dim + dim * dim), 2 * dim + 2 * dim * dim
+
+
 def pack(x, v, F, C) -> torch.Tensor:
-    """Row-major x[n,3], v[n,3], F[n,3,3], C[n,3,3] -> one component-major [24, n] buffer."""
-    n = x.shape[0]
-    return torch.cat([x.reshape(n, 3).t(), v.reshape(n, 3).t(), F.reshape(n, 9).t(), C.reshape(n, 9).t()],
+    """Row-major x[n,d], v[n,d], F[n,d,d], C[n,d,d] -> one component-major [2d + 2d^2, n] buffer."""
+    n, d = x.shape[0], x.shape[-1]
+    return torch.cat([x.reshape(n, d).t(), v.reshape(n, d).t(), F.reshape(n, d * d).t(), C.reshape(n, d * d).t()],
                      dim=0).contiguous()
 
 
 def unpack(buf: torch.Tensor):
     n = buf.shape[1]
-    x = buf[0:3].t().contiguous()
-    v = buf[3:6].t().contiguous()
-    F = buf[6:15].t().contiguous().reshape(n, 3, 3)
-    C = buf[15:24].t().contiguous().reshape(n, 3, 3)
+    d = 3 if buf.shape[0] == 24 else 2
+    (ox, ov, oF, oC), rows = _rows(d)
+    x = buf[ox:ov].t().contiguous()
+    v = buf[ov:oF].t().contiguous()
+    F = buf[oF:oC].t().contiguous().reshape(n, d, d)
+    C = buf[oC:rows].t().contiguous().reshape(n, d, d)
     return x, v, F, C
 
 
 class _Runner:
     """The C-ABI calls of one rollout: forward substeps and adjoint substeps on [24, n] buffers."""
 
-    def __init__(self, cfg: RolloutConfig, n: int, dtype, device, mass, mu_0, lambda_0):
+    def __init__(self, cfg: RolloutConfig, n: int, dtype, device, mass, mu_0, lambda_0, dim: int = 3):
         self.n = n
+        self.dim = dim
         self.dtype = dtype
         self.device = device
-        self.params = E.make_params(3, cfg.res, dtype, 1.0 / cfg.res, float(cfg.res), cfg.dt, cfg.gravity,
+        self.params = E.make_params(dim, cfg.res, dtype, 1.0 / cfg.res, float(cfg.res), cfg.dt, cfg.gravity,
                                     cfg.volume, cfg.hardening, model=cfg.model, wall_mode=cfg.wall_mode,
                                     planes=cfg.planes, plane_rule=cfg.plane_rule)
         if torch.is_tensor(mass):
@@ -95,7 +105,7 @@ class _Runner:
         P = N.Particles()
         P.n, P.stride = self.n, self.n
         base, es = buf.data_ptr(), buf.element_size()
-        P.x, P.v, P.F, P.C = (base + es * self.n * r0 for r0 in (0, 3, 6, 15))
+        P.x, P.v, P.F, P.C = (base + es * self.n * r0 for r0 in _rows(self.dim)[0])
         P.Jp = self.Jp.data_ptr()
         P.mass = self.mass.data_ptr() if self.mass is not None else None
         P.mu_0, P.lambda_0 = self.mu.data_ptr(), self.lam.data_ptr()
@@ -110,7 +120,7 @@ class _Runner:
         P = self._particles(state)
         A = N.Adjoint()
         base, es = adj.data_ptr(), adj.element_size()
-        A.x, A.v, A.F, A.C = (base + es * self.n * r0 for r0 in (0, 3, 6, 15))
+        A.x, A.v, A.F, A.C = (base + es * self.n * r0 for r0 in _rows(self.dim)[0])
         A.mu_0, A.lambda_0 = mu_bar.data_ptr(), lam_bar.data_ptr()
         N.call("ffmpm_substep_adjoint", ctypes.byref(self.params), ctypes.byref(P), ctypes.byref(A),
                ctypes.c_void_p(self.adj_ptr), ctypes.c_size_t(self.adj_bytes.value), self.stream)
@@ -136,7 +146,7 @@ class MPMRollout(torch.autograd.Function):
     def forward(ctx, x0, v0, F0, C0, mu_0, lambda_0, mass, cfg: RolloutConfig):
         n = x0.shape[0]
         ctx.scalar_mu, ctx.scalar_lam = mu_0.dim() == 0, lambda_0.dim() == 0
-        runner = _Runner(cfg, n, x0.dtype, x0.device, mass, mu_0.expand(n), lambda_0.expand(n))
+        runner = _Runner(cfg, n, x0.dtype, x0.device, mass, mu_0.expand(n), lambda_0.expand(n), dim=x0.shape[1])
         buf = pack(x0.detach(), v0.detach(), F0.detach(), C0.detach())
         K = max(1, int(cfg.checkpoint_every))
         ckpts = []
@@ -156,11 +166,12 @@ class MPMRollout(torch.autograd.Function):
         def z(g, shape):
             return torch.zeros(shape, dtype=dtype, device=dev) if g is None else g.to(dtype)
 
-        adj = pack(z(gx, (n, 3)), z(gv, (n, 3)), z(gF, (n, 3, 3)), z(gC, (n, 3, 3)))
+        d = runner.dim
+        adj = pack(z(gx, (n, d)), z(gv, (n, d)), z(gF, (n, d, d)), z(gC, (n, d, d)))
         mu_bar = torch.zeros(n, dtype=torch.float64, device=dev)
         lam_bar = torch.zeros(n, dtype=torch.float64, device=dev)
         K = max(1, int(cfg.checkpoint_every))
-        seg = torch.empty((min(K, cfg.steps), 24, n), dtype=dtype, device=dev)
+        seg = torch.empty((min(K, cfg.steps), _rows(d)[1], n), dtype=dtype, device=dev)
         for si in reversed(range(len(ckpts))):
             count = min(K, cfg.steps - si * K)
             seg[0].copy_(ckpts[si])
@@ -180,17 +191,17 @@ class MPMRollout(torch.autograd.Function):
 def simulate(x0, v0, mu_0, lambda_0, cfg: RolloutConfig, mass, F0=None, C0=None):
     """Differentiable rollout of cfg.steps substeps; returns (x, v, F, C) at the end.
 
-    x0, v0: [n, 3] CUDA tensors (float32 or float64); mu_0, lambda_0: scalars / 0-dim tensors (one
+    x0, v0: [n, 3] (3D) or [n, 2] (2D) CUDA tensors (float32 or float64); mu_0, lambda_0: scalars / 0-dim tensors (one
     material) or [n] tensors (autograd-tracked, e.g. from ``lame(E, nu)``); mass: float or [n]
     tensor (not differentiated).
     F0, C0 default to the reference's initial state (identity, zero; mls_mpm.py:9-15).
     """
-    n = x0.shape[0]
+    n, d = x0.shape[0], x0.shape[1]
     dtype, dev = x0.dtype, x0.device
     if F0 is None:
-        F0 = torch.eye(3, dtype=dtype, device=dev).expand(n, 3, 3)
+        F0 = torch.eye(d, dtype=dtype, device=dev).expand(n, d, d)
     if C0 is None:
-        C0 = torch.zeros((n, 3, 3), dtype=dtype, device=dev)
+        C0 = torch.zeros((n, d, d), dtype=dtype, device=dev)
     mu = torch.as_tensor(mu_0, dtype=dtype, device=dev)
     lam = torch.as_tensor(lambda_0, dtype=dtype, device=dev)
     return MPMRollout.apply(x0, v0, F0, C0, mu, lam, mass, cfg)

@@ -316,7 +316,7 @@ int ffmpm_batch2d_status(void *ws, int32_t *status, void *stream);
  * partial results.  No reference counterpart. */
 int ffmpm_batch2d_set_waits(void *ws, uint32_t wait_limit, uint32_t inject, void *stream);
 
-/* ---- adjoint of one 3D substep (reverse mode, for differentiable rollouts) ---- */
+/* ---- adjoint of one 3D or 2D substep (reverse mode, for differentiable rollouts) ---- */
 
 /* Adjoints of a particle state, laid out exactly like the ffmpm_particles they belong to (same
  * real type, same `stride`).  On entry x, v, F, C hold dL/d(state after the substep); on return
@@ -328,18 +328,21 @@ typedef struct ffmpm_adjoint {
   double *mu_0, *lambda_0;
 } ffmpm_adjoint;
 
-/* Workspace bytes of ffmpm_substep_adjoint (status header + two dense (res+1)^3 grids of float64
- * nodes, 32 bytes each, for either real type). */
+/* Workspace bytes of ffmpm_substep_adjoint (status header + three dense (res+1)^dim grids of
+ * 32-byte nodes, for either real type).  dim other than 2 or 3: FFMPM_ERR_UNSUPPORTED. */
 int ffmpm_adjoint_workspace_size(const ffmpm_params *p, int64_t n, size_t *bytes);
 
-/* Reverse of one ffmpm_substep (3D, model FFMPM_MODEL_NEO_HOOKEAN or FFMPM_MODEL_FIXED_COROTATED, either
- * wall mode) at the state
- * P (the state BEFORE the substep; P is only read).  The substep's grid is recomputed from P, then
- * G2P is reversed as a scatter of node-velocity adjoints, the grid update as a per-node rule (the
- * division by mass, the clamp and the walls pass no gradient where they clip), and P2G as a gather
- * that also differentiates the stress, including the polar factor.  The workspace's status header
- * reads with ffmpm_status_read.  Other dims/models: FFMPM_ERR_UNSUPPORTED.  The reference has no
- * derivative; this is the exact derivative of solve_mls_mpm_3d (mls_mpm.py:40-79). */
+/* Reverse of one ffmpm_substep (3D or 2D, model FFMPM_MODEL_NEO_HOOKEAN or
+ * FFMPM_MODEL_FIXED_COROTATED, either wall mode) at the state P (the state BEFORE the substep; P is
+ * only read).  The substep's grid is recomputed from P, then G2P is reversed as a scatter of
+ * node-velocity adjoints, the grid update as a per-node rule (the division by mass, the clamp and
+ * the walls pass no gradient where they clip; in 2D the y < 0.05 band passes v_y's adjoint only
+ * where v_y > 0), and P2G as a gather that also differentiates the stress, including the polar
+ * factor (3D) or the closed-form rotation (2D).  Jp is not differentiated (it does not feed back
+ * for these models).  The workspace's status header reads with ffmpm_status_read.  Other
+ * dims/models (snow): FFMPM_ERR_UNSUPPORTED.  The reference has no derivative; this is the exact
+ * derivative of solve_mls_mpm_3d (mls_mpm.py:40-79) and of the 2D substep (two_d/p2g.py,
+ * grid_op.py, g2p.py). */
 int ffmpm_substep_adjoint(const ffmpm_params *p, const ffmpm_particles *P, ffmpm_adjoint *A, void *ws,
                           size_t ws_bytes, void *stream);
 

@@ -3,7 +3,7 @@
 * its forward half equals the C oracle's substep (itself pinned to the reference's goldens);
 * its reverse half equals FP64 central differences of that forward, for every input of the
   substep (x, v, F, C) and for the Lamé parameters, one substep and a short rollout;
-* the C-ABI rejects what the adjoint does not cover (2D, snow) without touching a GPU.
+* the C-ABI rejects what the adjoint does not cover (snow, other dims) without touching a GPU.
 """
 import ctypes
 import os
@@ -137,10 +137,18 @@ def test_capi_rejects_unsupported_adjoints():
     if not os.path.exists(N.LIB_PATH):
         pytest.skip("library not built")
     lib = N.load()
-    p = N.Params(dim=2, res=32, real_bytes=4, dx=1 / 32, inv_dx=32.0, dt=1e-4, volume=1.0, hardening=1.0)
+    p = N.Params(dim=4, res=32, real_bytes=4, dx=1 / 32, inv_dx=32.0, dt=1e-4, volume=1.0, hardening=1.0)
     out = ctypes.c_size_t(0)
     assert lib.ffmpm_adjoint_workspace_size(ctypes.byref(p), 10, ctypes.byref(out)) == N.ERR_UNSUPPORTED
     P, A = N.Particles(), N.Adjoint()
+    assert lib.ffmpm_substep_adjoint(ctypes.byref(p), ctypes.byref(P), ctypes.byref(A), None, 0, None) == \
+        N.ERR_UNSUPPORTED
+    p.dim = 2  # 2D elastic: three (res+1)^2 grids of 32-byte nodes
+    assert lib.ffmpm_adjoint_workspace_size(ctypes.byref(p), 10, ctypes.byref(out)) == N.OK
+    assert out.value >= 256 + 3 * 32 * 33 ** 2
+    assert lib.ffmpm_substep_adjoint(ctypes.byref(p), ctypes.byref(P), ctypes.byref(A), None, 0, None) == \
+        N.ERR_WORKSPACE
+    p.model = N.MODELS["snow"]
     assert lib.ffmpm_substep_adjoint(ctypes.byref(p), ctypes.byref(P), ctypes.byref(A), None, 0, None) == \
         N.ERR_UNSUPPORTED
     p.dim, p.model = 3, N.MODELS["snow"]
@@ -151,6 +159,6 @@ def test_capi_rejects_unsupported_adjoints():
         N.ERR_UNSUPPORTED
     p.model = N.MODELS["fixed_corotated"]
     assert lib.ffmpm_adjoint_workspace_size(ctypes.byref(p), 10, ctypes.byref(out)) == N.OK
-    assert out.value >= 256 + 2 * 16 * 33 ** 3
+    assert out.value >= 256 + 3 * 32 * 33 ** 3
     assert lib.ffmpm_substep_adjoint(ctypes.byref(p), ctypes.byref(P), ctypes.byref(A), None, 0, None) == \
         N.ERR_WORKSPACE
