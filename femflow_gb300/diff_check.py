@@ -211,6 +211,32 @@ def run(n=131072, res=64, steps=2000, every=50, dt=1e-4, E_mod=4e3, nu=0.3, seed
     return report
 
 
+def time_backward(n=131072, res=64, steps=400, every=50, dt=1e-4, E_mod=4e3, nu=0.3, seed=0,
+                  model="fixed_corotated", reps=2, device="cuda") -> dict:
+    """Wall time of the float32 forward and backward of the spread loss over `steps` substeps of the
+    cube scene (CUDA-synchronised), best of `reps`; no finite differences."""
+    dev = torch.device(device)
+    x0, v0, direction, vol, F0 = cube_scene(n, seed=seed)
+    cfg = RolloutConfig(res=res, dt=dt, steps=steps, volume=vol, checkpoint_every=every, model=model)
+    best = None
+    for _ in range(reps):
+        E = torch.tensor(E_mod, dtype=torch.float64, device=dev, requires_grad=True)
+        nuv = torch.tensor(nu, dtype=torch.float64, device=dev, requires_grad=True)
+        v = torch.as_tensor(v0, dtype=torch.float32, device=dev).requires_grad_(True)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        xs, _, Fs, _ = _rollout(x0, v, E, nuv, cfg, 1.0 * vol, torch.float32, dev, F0)
+        torch.cuda.synchronize(dev)
+        t1 = time.perf_counter()
+        losses(xs, Fs)["spread"].backward()
+        torch.cuda.synchronize(dev)
+        t2 = time.perf_counter()
+        r = dict(forward_s=t1 - t0, backward_s=t2 - t1, backward_ms_per_substep=(t2 - t1) / steps * 1e3,
+                 dE=E.grad.item(), dnu=nuv.grad.item())
+        best = r if best is None or r["backward_s"] < best["backward_s"] else best
+    return dict(n=n, res=res, steps=steps, checkpoint_every=every, **best)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--n", type=int, default=131072)
@@ -223,7 +249,12 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--model", default="fixed_corotated", choices=("fixed_corotated", "neo_hookean"))
     ap.add_argument("--f0-std", type=float, default=0.0, help="initial deformation: F0 = I + N(0, s^2)")
+    ap.add_argument("--time-backward", action="store_true",
+                    help="only time the float32 forward and backward of the spread loss (no finite differences)")
     a = ap.parse_args(argv)
+    if a.time_backward:
+        print(json.dumps(time_backward(a.n, a.res, a.steps, a.every, a.dt, a.E, a.nu, a.seed, a.model)))
+        return
     r = run(a.n, a.res, a.steps, a.every, a.dt, a.E, a.nu, a.seed, a.model, a.f0_std)
     print(json.dumps(r, indent=1, default=float))
 
