@@ -286,7 +286,7 @@ def run_ours(args):
         mls_mpm.solve_mls_mpm_3d(RES, float(RES), 1.0, 1 / RES, DT, s["vol"], GRAVITY, pset, v_h, F_h, C_h, J_h)
     torch.cuda.synchronize(dev)
     te = REP.max_over_ranks(time.perf_counter() - e0, dev)
-    out["e2e"] = {"value": world * n * e2e_steps / te, "unit": UNIT, "h2d_bytes_per_step": n * (12 + 12 + 12 + 36 + 36 + 4),
+    out["e2e"] = {"value": world * n * e2e_steps / te, "unit": UNIT, "h2d_bytes_per_step": n * (12 + 12 + 12 + 36 + 36),
                   "d2h_bytes_per_step": n * (12 + 12 + 36 + 36), "steps": e2e_steps,
                   "api": "solve_mls_mpm_3d on pinned host float32 arrays (ffmpm_substep_host: uploads, scatter, "
                          "gather and downloads pipelined over chunks of particles)"}

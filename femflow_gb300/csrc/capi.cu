@@ -508,23 +508,25 @@ int op_substep_host(const ffmpm_params& p, const Layout& L, const Ws& w, const f
     void* h;
     void* d;
     size_t per;   // bytes per particle
+    bool in;      // read by the substep
     bool out;     // written by the substep
     bool whole;   // one real per particle: sent up whole before the first chunk (fewer, larger copies)
   };
-  // Jp changes only in 2D and for snow (three_d/g2p.py:48-58): elsewhere it is not sent back
-  const bool jp_out = DIM == 2 || p.model == FFMPM_MODEL_SNOW;
-  const Arr arrs[8] = {{H->x, D->x, DIM * rb, true, false},
-                       {H->v, D->v, DIM * rb, true, false},
-                       {H->F, D->F, DIM * DIM * rb, true, false},
-                       {H->C, D->C, DIM * DIM * rb, true, false},
-                       {H->Jp, D->Jp, rb, jp_out, true},
-                       {const_cast<void*>(H->mass), const_cast<void*>(D->mass), rb, false, true},
-                       {const_cast<void*>(H->mu_0), const_cast<void*>(D->mu_0), rb, false, true},
-                       {const_cast<void*>(H->lambda_0), const_cast<void*>(D->lambda_0), rb, false, true}};
+  // Jp is read and changed only in 2D and for snow (two_d/g2p.py:44-46, three_d/p2g.py:57-61,
+  // three_d/g2p.py:48-58): elsewhere it is neither sent up nor sent back
+  const bool jp_used = DIM == 2 || p.model == FFMPM_MODEL_SNOW;
+  const Arr arrs[8] = {{H->x, D->x, DIM * rb, true, true, false},
+                       {H->v, D->v, DIM * rb, true, true, false},
+                       {H->F, D->F, DIM * DIM * rb, true, true, false},
+                       {H->C, D->C, DIM * DIM * rb, true, true, false},
+                       {H->Jp, D->Jp, rb, jp_used, jp_used, true},
+                       {const_cast<void*>(H->mass), const_cast<void*>(D->mass), rb, true, false, true},
+                       {const_cast<void*>(H->mu_0), const_cast<void*>(D->mu_0), rb, true, false, true},
+                       {const_cast<void*>(H->lambda_0), const_cast<void*>(D->lambda_0), rb, true, false, true}};
   // copies of [a, b) of the chunked arrays (whole = false: the per-particle scalars over [0, n))
   auto copy = [&](bool down, int64_t a, int64_t b, cudaStream_t cs, bool whole = false) {
     for (const Arr& r : arrs) {
-      if (!r.h || (down && !r.out) || (!down && r.whole != whole)) continue;
+      if (!r.h || (down && !r.out) || (!down && (!r.in || r.whole != whole))) continue;
       unsigned char* hb = static_cast<unsigned char*>(r.h) + a * r.per;
       unsigned char* db = static_cast<unsigned char*>(r.d) + a * r.per;
       if (down)

@@ -133,3 +133,41 @@ def test_host_substep_2d_through_the_c_abi(dtype):
     close(n(x), xo, 5 * tol["x"], scale=1.0, what="x")
     close(n(v), vo, 5 * tol["v"], scale=np.abs(vo).max() + abs(grav * dt), what="v")
     close(sign_align(n(F), Fo), Fo, 5 * tol["F"], scale=1.0, what="F")
+
+
+def test_host_substep_3d_snow_sends_jp_both_ways():
+    """Snow on host arrays (hardening from Jp in P2G, the singular-value clamp and the Jp update in
+    G2P, three_d/p2g.py:57-61 and g2p.py:48-58): Jp goes up and comes back every substep, and the
+    result matches the oracle's snow substep; the elastic model leaves the host Jp untouched."""
+    s = two_cubes(1500, 24, seed=6)
+    res, dt, g, h = 24, 1e-4, -9.8, 10.0
+    N_ = len(s["x"])
+    rng = np.random.default_rng(6)
+    F0 = np.tile(np.eye(3), (N_, 1, 1)) + rng.normal(0, 0.02, (N_, 3, 3))
+    Jp0 = rng.uniform(0.9, 1.1, (N_, 1))
+    for model in ("snow", "neo_hookean"):
+        x, v, F, C, Jp = (pinned(a, torch.float64) for a in (s["x"], s["v"], F0, np.zeros((N_, 3, 3)), Jp0))
+        mass, mu, lam = (pinned(s[k], torch.float64) for k in ("mass", "mu", "lam"))
+        dev = [torch.empty_like(a, device="cuda") for a in (x, v, F, C, Jp, mass, mu, lam)]
+        prm = E.make_params(3, res, torch.float64, 1 / res, float(res), dt, g, s["vol"], h, model=model)
+        host = E.particles_struct(x, v, F, C, Jp, mass, mu, lam)
+        ds = E.particles_struct(*dev)
+        ws = E.workspace_for(prm, N_, torch.device("cuda"))
+        for _ in range(3):
+            N.call("ffmpm_substep_host", ctypes.byref(prm), ctypes.byref(host), ctypes.byref(ds),
+                   ctypes.c_void_p(ws.ptr), ctypes.c_size_t(ws.bytes),
+                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        torch.cuda.synchronize()
+        ws.raise_on_status()
+        xo, vo, Fo, Co, Jo = s["x"].copy(), s["v"].copy(), F0.copy(), np.zeros((N_, 3, 3)), Jp0.copy()
+        for _ in range(3):
+            O.substep_3d(res, float(res), h, 1 / res, dt, s["vol"], g, xo, s["mass"].copy(), s["mu"].copy(),
+                         s["lam"].copy(), vo, Fo, Co, Jo, model=model)
+        tol = TOL[torch.float64]
+        close(n(x), xo, 5 * tol["x"], scale=1.0, what=f"{model} x")
+        close(n(F), Fo, 20 * tol["F"], scale=1.0, what=f"{model} F")
+        if model == "snow":
+            assert np.abs(Jo - Jp0).max() > 1e-6  # the clamp moved some Jp
+            close(n(Jp), Jo, 20 * tol["F"], scale=1.0, what="snow Jp")
+        else:
+            assert np.array_equal(n(Jp), Jp0)
