@@ -351,10 +351,22 @@ int launch_corrector(const ffmpm_params& p, const ffmpm_grid& g, ffmpm_particles
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
     attr = true;
   }
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreadsC, smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreadsC, smem) != cudaSuccess) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  {
+    // CTAs per SM that the shared memory holds (each CTA also takes 1 KB reserved by the system)
+    int dev = 0, smem_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    const int by_smem = smem_sm / (int)(smem + 2048);
+    per_sm = std::max(per_sm, std::min(by_smem, 4));
+  }
   const int64_t tiles = (Pp.n + 127) / 128;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(tiles, int64_t(sm_count()) * std::max(1, per_sm)));
   ffmpm_mlp nn{};

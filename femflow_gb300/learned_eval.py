@@ -186,6 +186,39 @@ def run(res=128, dt=5e-5, ratio=8, scenes=16, per_cube=524288, samples=4, steps=
     return rep
 
 
+def profile_case(n_per_cube: int = 524288, res: int = 128, batch: int = 65536, seed: int = 0) -> dict:
+    """The corrector's tensor-core kernels on the full-size scene, for a profiler: 3 coarse steps with
+    an untrained network (strength 1e-3, so the state stays near the plain coarse step), then 2 more
+    (`k_corrector`: G2P fused with the 4-layer MLP), then one training forward and backward of a
+    batch (`k_tc_gemm`)."""
+    torch.manual_seed(seed)
+    st = L.Stepper(L.SceneSpec(n_per_cube=n_per_cube, E=120.0, seed=seed), res=res)
+    net = L.Net(max_batch=batch, seed=seed)
+    cor = L.Corrector(net, st, strength=1e-3)
+    buf = st.initial_state()
+    for _ in range(3):
+        st.coarse_step(buf, cor)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(2):
+        st.coarse_step(buf, cor)
+    e1.record()
+    torch.cuda.synchronize()
+    st.check()
+    coarse_ms = e0.elapsed_time(e1) / 2
+    X = torch.randn(batch, L.N.MLP_IN, device="cuda").to(torch.bfloat16)
+    T = torch.randn(batch, 12, device="cuda")
+    w = torch.tensor(L.OUT_WEIGHTS, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    net.forward_train(X)
+    net.backward_train(T, w, loss)
+    torch.cuda.synchronize()
+    net.check()
+    return {"particles": st.n, "coarse_steps": 5, "coarse_step_ms": coarse_ms, "train_batch": batch,
+            "loss": float(loss.item())}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--res", type=int, default=128)
@@ -202,7 +235,12 @@ def main(argv=None):
     ap.add_argument("--n-per-cube", type=int, default=524288)
     ap.add_argument("--E", type=float, default=120.0)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--profile-case", action="store_true",
+                    help="only run the corrector's tensor-core kernels on the full-size scene (for a profiler)")
     a = ap.parse_args(argv)
+    if a.profile_case:
+        print(json.dumps(profile_case(a.n_per_cube, a.res, seed=a.seed)))
+        return
     r = run(a.res, a.dt, a.ratio, a.scenes, a.per_cube, a.samples, a.steps, a.batch, a.horizon, a.n_per_cube, a.E,
             seed=a.seed, onpolicy_rounds=a.onpolicy_rounds, keep=a.keep)
     print(json.dumps(r, indent=1, default=float))
