@@ -188,13 +188,26 @@ class MPMRollout(torch.autograd.Function):
         return gx0, gv0, gF0, gC0, g_mu.to(dtype), g_lam.to(dtype), None, None
 
 
-def simulate(x0, v0, mu_0, lambda_0, cfg: RolloutConfig, mass, F0=None, C0=None):
+def cell_order(x: torch.Tensor, res: int) -> torch.Tensor:
+    """Stable order of particles by base cell (the node a particle's stencil starts at)."""
+    R = res + 1
+    b = torch.clamp(torch.floor(x.detach() * res - 0.5), -1, res).to(torch.int64) + 1
+    key = b[:, 0]
+    for a in range(1, x.shape[1]):
+        key = key * (R + 2) + b[:, a]
+    return torch.argsort(key, stable=True)
+
+
+def simulate(x0, v0, mu_0, lambda_0, cfg: RolloutConfig, mass, F0=None, C0=None, order: bool = True):
     """Differentiable rollout of cfg.steps substeps; returns (x, v, F, C) at the end.
 
     x0, v0: [n, 3] (3D) or [n, 2] (2D) CUDA tensors (float32 or float64); mu_0, lambda_0: scalars / 0-dim tensors (one
     material) or [n] tensors (autograd-tracked, e.g. from ``lame(E, nu)``); mass: float or [n]
     tensor (not differentiated).
     F0, C0 default to the reference's initial state (identity, zero; mls_mpm.py:9-15).
+    With ``order`` the rollout runs on the particles ordered by base cell (neighbouring lanes of the
+    adjoint kernels then share stencil nodes); inputs and outputs stay in the caller's order, and
+    autograd carries the permutation.
     """
     n, d = x0.shape[0], x0.shape[1]
     dtype, dev = x0.dtype, x0.device
@@ -204,4 +217,11 @@ def simulate(x0, v0, mu_0, lambda_0, cfg: RolloutConfig, mass, F0=None, C0=None)
         C0 = torch.zeros((n, d, d), dtype=dtype, device=dev)
     mu = torch.as_tensor(mu_0, dtype=dtype, device=dev)
     lam = torch.as_tensor(lambda_0, dtype=dtype, device=dev)
-    return MPMRollout.apply(x0, v0, F0, C0, mu, lam, mass, cfg)
+    if not order or n < 2:
+        return MPMRollout.apply(x0, v0, F0, C0, mu, lam, mass, cfg)
+    perm = cell_order(x0, cfg.res)
+    inv = torch.empty_like(perm)
+    inv[perm] = torch.arange(n, device=perm.device)
+    pick = lambda t: t[perm] if torch.is_tensor(t) and t.dim() >= 1 and t.shape[0] == n else t
+    out = MPMRollout.apply(pick(x0), pick(v0), pick(F0), pick(C0), pick(mu), pick(lam), pick(mass), cfg)
+    return tuple(o[inv] for o in out)
