@@ -76,7 +76,7 @@ def corrector_for(net, st, choice):
 
 def run(res=128, dt=5e-5, ratio=8, scenes=16, per_cube=524288, samples=4, steps=4000, batch=32768, horizon=150,
         n_per_cube=524288, E_eval=120.0, E_range=(50.0, 200.0), seed=0, onpolicy_rounds=3, onpolicy_samples=8,
-        onpolicy_gap=10, round_steps=None, keep=1.0 / 16) -> dict:
+        onpolicy_gap=10, round_steps=None, keep=1.0 / 16, max_target=30.0) -> dict:
     rep = dict(res=res, dt_fine=dt, ratio=ratio, dt_coarse=dt * ratio, horizon_coarse_steps=horizon,
                simulated_time=horizon * ratio * dt, E_range=E_range, E_eval=E_eval, model="fixed_corotated")
     t0 = time.perf_counter()
@@ -110,6 +110,14 @@ def run(res=128, dt=5e-5, ratio=8, scenes=16, per_cube=524288, samples=4, steps=
         if Xo is None:  # every scene left the grid: no samples this round
             rep["onpolicy"].append(dict(round=rnd + 1, strength=a, samples=int(X.shape[0]), scenes_left_grid=dropped))
             continue
+        # a corrected trajectory can blow up locally without leaving the grid; the fine rollout from
+        # such a state gives targets far outside what the network is meant to learn, and a few of them
+        # dominate the squared loss.  Rows beyond `max_target` standard deviations of the fine-rollout
+        # targets (or not finite) are dropped.
+        ts = (To / net.out_scale[:12]).abs().amax(dim=1)
+        ok = torch.isfinite(ts) & (ts < max_target) & torch.isfinite(Xo.float()).all(dim=1)
+        rows_dropped = int((~ok).sum())
+        Xo, To = Xo[ok], To[ok]
         X, T = torch.cat([X, Xo]), torch.cat([T, To])
         del Xo, To
         Xs, Ts = L.scaled(net, X, T)
@@ -117,7 +125,7 @@ def run(res=128, dt=5e-5, ratio=8, scenes=16, per_cube=524288, samples=4, steps=
         del Xs, Ts
         torch.cuda.synchronize()
         rep["onpolicy"].append(dict(round=rnd + 1, strength=a, samples=int(X.shape[0]), scenes_left_grid=dropped,
-                                    seconds=time.perf_counter() - t1))
+                                    rows_dropped=rows_dropped, seconds=time.perf_counter() - t1))
     del X, T
     torch.cuda.synchronize()
     rep["train_seconds"] = time.perf_counter() - t0
