@@ -6,7 +6,7 @@
 // adjoints of x', v', F', C', runs five kernels on a dense (res+1)^3 grid:
 //   k_adj_p2g      recompute the substep's grid (momentum, mass) from the input state
 //   k_adj_gridvel  the grid update of every node once: updated velocity (and mass) for the gathers
-//   k_adj_g2p      reverse G2P: per particle, scatter the node-velocity adjoints (one vector red per
+//   k_adj_g2p      reverse G2P: per particle, scatter the node-velocity adjoints (float64 adds per
 //                  stencil node) and form dL/dx, dL/dF of the gather and of F' = (I + dt C') F
 //   k_adj_grid     reverse grid update per node: division by mass, gravity, clamp and walls (the
 //                  clamp and the walls pass no gradient where they clip)
@@ -14,17 +14,18 @@
 //                  weights, the APIC momentum and the stress, including the polar factor R of F:
 //                  for F = R S, dL/dF gains R [y]_x with (tr(S) I - S) y = axial(R^T dL/dR).
 //
-// Both node grids are float64 for float particle states too, and every node contribution is formed
-// in float64 from float factors (a product of two floats is exact in double).  For float states,
-// the grids the particle kernels read back (updated velocities, node adjoints) are stored as float
-// pairs hi + lo (hi = the float nearest the double, lo = the float nearest the rest): a stencil
-// node's deviation from the stencil's centre node, (hi - hi_c) + (lo - lo_c), is then formed in
-// float with the accuracy of the double subtraction rounded to float (hi - hi_c is exact when the
-// two are within a factor two), without the float64 pipe.  Double states keep double grids.  The adjoints carry a
-// large, nearly uniform part (a body's bulk motion); the stress derivative needs only its variation
-// across a stencil, sum W (g_i - g) (x) dpos_i.  With float node sums, rounding that differs from
-// node to node (in the momentum and in the mass it is divided by) leaves ~1e-7 of the bulk part in
-// that variation, which biased float E- and nu-gradients of 2000-substep rollouts by ~1%.
+// The adjoints carry a large, nearly uniform part (a body's bulk motion); the stress derivative
+// needs only its variation across a stencil, sum W (g_i - g) (x) dpos_i.  With float node sums,
+// rounding that differs from node to node (in the momentum and in the mass it is divided by) leaves
+// ~1e-7 of the bulk part in that variation, which biased float E- and nu-gradients of 2000-substep
+// rollouts by ~1%.  So the grids are accumulated in float64 for float particle states too, every
+// node contribution formed in float64 from float factors (a product of two floats is exact in
+// double).  For float states the grids the particle kernels read back (updated velocities, node
+// adjoints) are then stored as float pairs hi + lo (hi = the float nearest the double, lo = the
+// float nearest the rest): a stencil node's deviation from the stencil's centre node,
+// (hi - hi_c) + (lo - lo_c), is formed in float with the accuracy of the double subtraction rounded
+// to float (hi - hi_c is exact when the two are within a factor two), without the float64 pipe.
+// Double states keep double grids throughout.
 #include <cuda_runtime.h>
 
 #include <algorithm>
