@@ -29,6 +29,18 @@ class Scene2D(ctypes.Structure):
                 ("mass", ctypes.c_double), ("mu_0", ctypes.c_double), ("lambda_0", ctypes.c_double)]
 
 
+def batch_cell_order(x: np.ndarray, offsets, res) -> np.ndarray:
+    """perm[i] = the caller's index (within the batch) of the particle at position i: every scene's
+    particles (x[offsets[s]:offsets[s+1]] on a res[s]^2 grid) stably ordered by base cell, scenes
+    kept in place."""
+    perm = []
+    for s, r in enumerate(res):
+        a, b = int(offsets[s]), int(offsets[s + 1])
+        cell = np.clip(np.floor(x[a:b] * r - 0.5), -1, r).astype(np.int64)
+        perm.append(a + np.argsort(cell[:, 0] * (r + 2) + cell[:, 1], kind="stable"))
+    return np.concatenate(perm) if perm else np.zeros(0, dtype=np.int64)
+
+
 class Batch2D:
     """``scenes``: list of dicts with ``x`` [n,2] and scalars ``res``, ``dt``, ``mass``, ``volume``,
     ``mu_0``, ``lambda_0`` (optional: ``v``, ``F``, ``C``, ``Jp``, ``gravity`` (-9.8),
@@ -54,15 +66,8 @@ class Batch2D:
         Jp = np.concatenate([np.asarray(s.get("Jp", np.ones(c)), dtype=np.float64).reshape(-1)
                              for s, c in zip(scenes, counts)])
         # each scene's particles in the order of their base cell: the kernel's P2G sums the
-        # contributions of a warp's lanes that share a cell before its atomics.  perm[i] is the
-        # caller's index (within the batch) of the particle at position i.
-        perm = []
-        for s, a, c in zip(scenes, self.offsets[:-1], counts):
-            res = int(s["res"])
-            xs = x[a:a + c]
-            cell = np.clip(np.floor(xs * res - 0.5), -1, res).astype(np.int64)
-            perm.append(a + np.argsort(cell[:, 0] * (res + 2) + cell[:, 1], kind="stable"))
-        perm = np.concatenate(perm) if perm else np.zeros(0, dtype=np.int64)
+        # contributions of a warp's lanes that share a cell before its atomics
+        perm = batch_cell_order(x, self.offsets, [int(s["res"]) for s in scenes])
         x, v, F, C, Jp = x[perm], v[perm], F[perm], C[perm], Jp[perm]
         self.perm = torch.as_tensor(perm, device=self.device)
         self._inv = torch.empty_like(self.perm)

@@ -122,3 +122,37 @@ def test_particle_count_limit():
     lib = N.load()
     assert lib.ffmpm_workspace_size(ctypes.byref(prm), (1 << 30) - 1, ctypes.byref(out)) == N.OK
     assert lib.ffmpm_workspace_size(ctypes.byref(prm), 1 << 30, ctypes.byref(out)) == N.ERR_BADARG
+
+
+def test_batch_cell_order_is_a_per_scene_stable_sort_by_base_cell():
+    from femflow_gb300.batched import batch_cell_order
+
+    rng = np.random.default_rng(3)
+    counts, res = [500, 0, 1300, 7], [32, 64, 128, 16]
+    offsets = np.concatenate([[0], np.cumsum(counts)])
+    x = rng.uniform(0.1, 0.9, (offsets[-1], 2))
+    perm = batch_cell_order(x, offsets, res)
+    assert sorted(perm.tolist()) == list(range(offsets[-1]))
+    for s, r in enumerate(res):
+        a, b = offsets[s], offsets[s + 1]
+        p = perm[a:b]
+        assert ((p >= a) & (p < b)).all()  # scenes stay in place
+        cell = np.floor(x[p] * r - 0.5).astype(np.int64)
+        key = cell[:, 0] * (r + 2) + cell[:, 1]
+        assert (np.diff(key) >= 0).all()
+        same = np.diff(key) == 0
+        assert (np.diff(p)[same] > 0).all()  # stable: equal cells keep the caller's order
+
+
+def test_rollout_cell_order_and_its_inverse():
+    import torch
+    from femflow_gb300.diff import cell_order
+
+    x = torch.rand(2000, 3, dtype=torch.float64)
+    p = cell_order(x, 16)
+    inv = torch.empty_like(p)
+    inv[p] = torch.arange(len(p))
+    assert torch.equal(x[p][inv], x)
+    b = (torch.floor(x[p] * 16 - 0.5) + 1).long()
+    key = (b[:, 0] * 19 + b[:, 1]) * 19 + b[:, 2]
+    assert (key[1:] >= key[:-1]).all()
