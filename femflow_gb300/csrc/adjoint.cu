@@ -38,7 +38,7 @@
 namespace ffmpm {
 namespace {
 
-constexpr int kAdjThreads = 256;
+constexpr int kAdjThreads = 128;
 
 template <typename T>
 struct AView {
