@@ -112,3 +112,27 @@ def test_rollout2d_gradients_match_fp64_central_differences():
         r32 = abs(grads[torch.float32][k] - fd[k]) / abs(fd[k])
         assert r64 <= 1e-5, (k, r64, grads, fd)
         assert r32 <= 1e-3, (k, r32, grads, fd)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_adjoint_of_no_particles_is_a_no_op(dim):
+    cfg = D.RolloutConfig(res=16, dt=1e-4, steps=1, volume=1e-5)
+    z = torch.zeros(0, dtype=torch.float32, device="cuda")
+    run = D._Runner(cfg, 0, torch.float32, torch.device("cuda"), 1e-5, z, z, dim=dim)
+    rows = 24 if dim == 3 else 12
+    state = torch.zeros((rows, 0), dtype=torch.float32, device="cuda")
+    adj = torch.zeros_like(state)
+    run.adjoint(state, adj, torch.zeros(0, dtype=torch.float64, device="cuda"),
+                torch.zeros(0, dtype=torch.float64, device="cuda"))
+    run.check()
+
+
+def test_rollout2d_of_one_particle_has_gradients():
+    cfg = D.RolloutConfig(res=32, dt=1e-4, steps=5, volume=1e-4, checkpoint_every=2)
+    x = torch.tensor([[0.5, 0.6]], dtype=torch.float64, device="cuda")
+    v = torch.tensor([[0.1, -0.2]], dtype=torch.float64, device="cuda", requires_grad=True)
+    xs, vs, _, _ = D.simulate(x, v, torch.tensor(400.0, dtype=torch.float64), torch.tensor(600.0, dtype=torch.float64),
+                              cfg, 1e-4)
+    xs[:, 0].sum().backward()
+    # a lone particle moves ballistically under gravity: dx/dv0 = total time along x
+    assert abs(float(v.grad[0, 0]) - 5 * 1e-4) < 1e-9

@@ -136,3 +136,27 @@ def test_batch_orders_particles_by_cell_and_maps_back():
         assert (np.diff(key) >= 0).all()
         k = 17 % len(s["x"])
         np.testing.assert_array_equal(n(b.x[:, b.position(i, k)]), s["x"][k])
+
+
+def test_batch_with_an_empty_scene():
+    """A scene without particles (zero-count entries in the particle offsets, an empty node box)
+    between scenes that have them: the others still match the oracle."""
+    sc = small_batch(seed=8)[:4]
+    empty = dict(sc[1])
+    empty["x"] = np.zeros((0, 2))
+    empty["v"] = np.zeros((0, 2))
+    sc = [sc[0], empty, sc[2], sc[3]]
+    b = Batch2D(sc, dtype=torch.float64)
+    b.step(3)
+    assert b.status() == 0
+    assert b.scene_state(1)["x"].shape == (0, 2)
+    for i in (0, 2, 3):
+        s = sc[i]
+        if s.get("wall_mode", "reference") != "reference":
+            continue
+        x = s["x"].copy(); v = s["v"].copy(); N_ = len(x)
+        F = np.tile(np.eye(2), (N_, 1, 1)); C = np.zeros((N_, 2, 2)); Jp = np.ones((N_, 1))
+        for _ in range(3):
+            O.substep_2d(s["res"], float(s["res"]), s.get("hardening", 1.0), s["mu_0"], s["lambda_0"], s["mass"],
+                         1.0 / s["res"], s["dt"], s["volume"], -9.8, x, v, F, C, Jp, s.get("model", "neo_hookean"))
+        close(n(b.scene_state(i)["x"]), x, 5 * TOL[torch.float64]["x"], scale=1.0, what=f"scene {i} x")
