@@ -61,6 +61,16 @@ def select(net: L.Net, spec: L.SceneSpec, res, dt, ratio, horizon) -> dict:
     return dict(best=best, trials=trials)
 
 
+def bounded_rows(X: torch.Tensor, T: torch.Tensor, out_scale: torch.Tensor, max_target: float):
+    """Samples (rows of X, T) whose targets stay within `max_target` output scales and whose
+    features and targets are finite, and the number of rows dropped.  A corrected trajectory can
+    blow up locally without leaving the grid; the fine rollout from such a state gives targets far
+    outside what the network is meant to learn, and a few of them dominate the squared loss."""
+    ts = (T / out_scale).abs().amax(dim=1)
+    ok = torch.isfinite(ts) & (ts < max_target) & torch.isfinite(X.float()).all(dim=1)
+    return X[ok], T[ok], int((~ok).sum())
+
+
 def velocity_corrector(net, st, strength):
     cor = L.Corrector(net, st, strength)
     cor.out_scale[0:9] = 0.0
@@ -110,14 +120,7 @@ def run(res=128, dt=5e-5, ratio=8, scenes=16, per_cube=524288, samples=4, steps=
         if Xo is None:  # every scene left the grid: no samples this round
             rep["onpolicy"].append(dict(round=rnd + 1, strength=a, samples=int(X.shape[0]), scenes_left_grid=dropped))
             continue
-        # a corrected trajectory can blow up locally without leaving the grid; the fine rollout from
-        # such a state gives targets far outside what the network is meant to learn, and a few of them
-        # dominate the squared loss.  Rows beyond `max_target` standard deviations of the fine-rollout
-        # targets (or not finite) are dropped.
-        ts = (To / net.out_scale[:12]).abs().amax(dim=1)
-        ok = torch.isfinite(ts) & (ts < max_target) & torch.isfinite(Xo.float()).all(dim=1)
-        rows_dropped = int((~ok).sum())
-        Xo, To = Xo[ok], To[ok]
+        Xo, To, rows_dropped = bounded_rows(Xo, To, net.out_scale[:12], max_target)
         X, T = torch.cat([X, Xo]), torch.cat([T, To])
         del Xo, To
         Xs, Ts = L.scaled(net, X, T)

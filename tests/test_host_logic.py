@@ -156,3 +156,18 @@ def test_rollout_cell_order_and_its_inverse():
     b = (torch.floor(x[p] * 16 - 0.5) + 1).long()
     key = (b[:, 0] * 19 + b[:, 1]) * 19 + b[:, 2]
     assert (key[1:] >= key[:-1]).all()
+
+
+def test_on_policy_rows_beyond_the_target_bound_are_dropped():
+    import torch
+    from femflow_gb300.learned_eval import bounded_rows
+
+    X = torch.randn(6, 128).to(torch.bfloat16)
+    T = torch.randn(6, 12)
+    T[1, 3] = 500.0           # far beyond the bound
+    T[4, 0] = float("nan")    # not finite
+    X[5, 7] = float("inf")    # feature not finite
+    scale = torch.full((12,), 2.0)
+    Xk, Tk, dropped = bounded_rows(X, T, scale, 30.0)
+    assert dropped == 3 and Xk.shape[0] == 3
+    assert torch.equal(Tk, T[[0, 2, 3]])
