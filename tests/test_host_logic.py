@@ -171,3 +171,35 @@ def test_on_policy_rows_beyond_the_target_bound_are_dropped():
     Xk, Tk, dropped = bounded_rows(X, T, scale, 30.0)
     assert dropped == 3 and Xk.shape[0] == 3
     assert torch.equal(Tk, T[[0, 2, 3]])
+
+
+def test_autotuner_picks_the_fastest_and_caches(tmp_path, monkeypatch):
+    from femflow_gb300 import autotune as AT
+
+    fake = {(128, 0): 3.0, (256, 0): 1.0, (512, 0): 2.0}
+    ran = []
+
+    def fake_time(fn, iters=3, warmup=1):
+        fn()
+        return fake[ran[-1]]
+
+    def run(c):
+        if c == (1024, 0):
+            raise RuntimeError("cannot launch")  # skipped, as a configuration that fails here
+        ran.append(c)
+
+    monkeypatch.setattr(AT, "time_call", fake_time)
+    monkeypatch.setattr(AT, "_CACHE", {})
+    monkeypatch.setenv("FFMPM_TUNE_CACHE", str(tmp_path / "tune.json"))
+    cands = [(128, 0), (1024, 0), (256, 0), (512, 0)]
+    best, timings = AT.tune(("sig", 1), cands, run)
+    assert best == (256, 0) and set(timings) == {(128, 0), (256, 0), (512, 0)}
+    # in-process cache: nothing runs again
+    ran.clear()
+    assert AT.tune(("sig", 1), cands, run) == ((256, 0), {}) and not ran
+    # a new process (empty in-process cache) reads the file cache
+    monkeypatch.setattr(AT, "_CACHE", {})
+    assert AT.tune(("sig", 1), cands, run) == ((256, 0), {}) and not ran
+    # no candidate can launch: an error, not a silent default
+    with pytest.raises(RuntimeError, match="no candidate"):
+        AT.tune(("sig", 2), [(1024, 0)], run)
