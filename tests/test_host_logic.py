@@ -203,3 +203,18 @@ def test_autotuner_picks_the_fastest_and_caches(tmp_path, monkeypatch):
     # no candidate can launch: an error, not a silent default
     with pytest.raises(RuntimeError, match="no candidate"):
         AT.tune(("sig", 2), [(1024, 0)], run)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_rollout_state_pack_round_trip(dim):
+    from femflow_gb300.diff import _rows, pack, unpack
+
+    n = 37
+    x, v = torch.randn(n, dim), torch.randn(n, dim)
+    F, C = torch.randn(n, dim, dim), torch.randn(n, dim, dim)
+    buf = pack(x, v, F, C)
+    (ox, ov, oF, oC), rows = _rows(dim)
+    assert buf.shape == (rows, n) and rows == 2 * dim + 2 * dim * dim
+    assert torch.equal(buf[ox:ov].t(), x) and torch.equal(buf[oC:rows].t().reshape(n, dim, dim), C)
+    for a, b in zip(unpack(buf), (x, v, F, C)):
+        assert torch.equal(a, b)
